@@ -1,0 +1,380 @@
+"""Benchmark of the FDTD wave-solver hot path on one GB300 (or N, as replicas).
+
+Workload (default): room_pillars -- a 20 x 15 x 8 m room with four pillars
+at a 500 Hz crossover (294 x 221 x 119 cells, 7.4 M air), five fitted
+frequency-dependent materials, one cardioid source (monopole + 3 dipoles =
+4 right-hand sides), 64 receivers plus a 1.2 m cut plane (4844 receivers),
+62 frequency bins, 1.0 s (8661 steps).  Seeded synthetic inputs.
+
+One bench step = one full run of that workload: all 8661 time steps of all 4
+right-hand sides, batched in one launch per time step, FP32.  The fields
+(2 x 135 MB per source chunk) are larger than L2 for the batched run.
+
+  value     air-cell updates per second over all right-hand sides, inputs
+            resident on the device (plan_run, CUDA events on the stream the
+            kernels run on), in G/s
+  e2e       the same metric through the C-ABI call wavey_cuda_fdtd_run_batch
+            with host buffers: packing, upload, run and read-back inside
+  roofline  the fused step kernel: 12 B per air-cell update per source
+            (read p, read and write the older buffer) / its mean launch time
+  plain     the same four right-hand sides run one at a time (S = 1 kernel)
+
+--impl reference times the reference's CPU algorithm (the oracle's C
+restatement of fdtd::run_cpu, FP64, OpenMP over z-slabs as the reference's
+rayon loop) on the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "FDTD Gcell-updates/s/source & HBM GB/s: batched vs plain, ≤0.1 dB vs FP64"
+UNIT = "Gcell-updates/s"
+BYTES_PER_UPDATE = 12  # FP32: read p^n, read p^(n-1), write p^(n+1)
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0):
+        self.device = device
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------- setup
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if os.environ.get("WAVEY_BENCH_GLOO") is None else "gloo"
+        if backend == "nccl":
+            import torch
+
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group(backend=backend)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v: float, world: int) -> float:
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload: str):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / f"fdtd_step_{workload}.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
+    return float(m.group(1)) if m else None
+
+
+def make_scene(workload: str, seed: int):
+    from wavey_gb300 import workloads as W
+
+    if workload == "room_pillars":
+        return W.room_pillars(seed=2)
+    if workload == "room_small":
+        return W.room_small(seed=1)
+    raise SystemExit(f"unknown workload {workload}")
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_sample(scene, sample_steps: int, threads: int = 0):
+    """Times the oracle (the reference's CPU loop) on the first sample_steps
+    steps of one right-hand side with every receiver and frequency."""
+    from oracle import fdtd as ofd
+
+    sig = scene.signal[:sample_steps]
+    t0 = time.perf_counter()
+    ofd.run(scene.grid, scene.sources[0], sig, scene.receivers, scene.freqs, "f64", threads=threads)
+    dt = time.perf_counter() - t0
+    updates = scene.grid.air * sample_steps
+    return updates / dt / 1e9, dt, ofd.max_threads() if threads == 0 else threads
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import build as obuild
+
+    obuild.build()
+    scene = make_scene(args.workload, 0)
+    sample = args.sample_steps
+    for _ in range(args.warmup):
+        cpu_sample(scene, sample)
+    vals, secs = [], []
+    cores = 1
+    for _ in range(args.steps):
+        v, dt, cores = cpu_sample(scene, sample)
+        vals.append(v)
+        secs.append(dt)
+    value = float(np.mean(vals))
+    desc = (f"{args.workload}: 1 of {len(scene.sources)} right-hand sides, first {sample} of {scene.steps} steps, "
+            f"all {len(scene.receivers)} receivers x {len(scene.freqs)} bins, FP64")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "notes": "the reference is Rust + wgpu and cannot be built here (no cargo/rustc); its CPU loop "
+                 "fdtd::run_cpu is timed through the oracle's C restatement on the host cores",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, rank, world):
+    from wavey_gb300 import _build
+
+    _build.build()
+    import torch
+
+    from wavey_gb300.backend import FP32, FP64, CudaBackend
+    from wavey_gb300 import workloads as W
+    from wavey_gb300.fdtd import to_transfer
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    scene = make_scene(args.workload, rank)
+    g = scene.grid
+    S = len(scene.sources)
+    b = CudaBackend(dev)
+    name, sms = b.device_info()
+    log(f"[rank {rank}] {name} ({sms} SMs): {scene.name} grid {g.n}, air {g.air}, {scene.steps} steps, S={S}, "
+        f"{len(scene.receivers)} receivers x {len(scene.freqs)} bins")
+    plan = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
+    info = plan.info()
+    log(f"[rank {rank}] plan: {info}")
+    for _ in range(args.warmup):
+        plan.run()
+    updates_per_run = g.air * scene.steps * S
+
+    barrier(world)
+    torch.cuda.synchronize()
+    step_ms = 0.0
+    launches = 0
+    total_ms = 0.0
+    chunks = 0
+    with ClockSampler(dev) as clocks:
+        for _ in range(args.steps):
+            st = plan.run(stats=True)
+            total_ms += st["total_ms"]
+            step_ms += st["step_ms"]
+            launches += st["step_launches"]
+            chunks = st["chunks"]
+    torch.cuda.synchronize()
+    barrier(world)
+    elapsed = max_over_ranks(total_ms / 1e3, world)
+    value = updates_per_run * args.steps * world / elapsed / 1e9
+    spec32 = plan.read()
+
+    # Roofline of the fused step kernel.
+    peak, peak_kind = peaks()
+    launch_s = step_ms / 1e3 / launches
+    alg_bytes = BYTES_PER_UPDATE * g.air * S
+    achieved = alg_bytes / launch_s / 1e9
+    traffic = profiled_traffic(args.workload)
+
+    # Plain: the same right-hand sides one at a time with the S = 1 kernel.
+    plain = None
+    if not args.no_plain:
+        t_plain = 0.0
+        for src in scene.sources:
+            p1 = b.plan(g, [src], scene.signal, scene.receivers, scene.freqs, FP32)
+            p1.run()
+            t_plain += p1.run(stats=True)["total_ms"] / 1e3
+            p1.close()
+        plain = updates_per_run / t_plain / 1e9
+
+    # End to end through the C-ABI with host buffers.
+    e2e_times = []
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run_batch(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(float(np.median(e2e_times)), world)
+    e2e = updates_per_run * world / e2e_s / 1e9
+
+    # Accuracy: FP32 against an FP64 GPU run of the same grid, as octave-band
+    # levels of the directional source's combined transfer function.
+    acc = None
+    if not args.no_accuracy:
+        p64 = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP64)
+        p64.run()
+        spec64 = p64.read()
+        p64.close()
+        h0 = np.ones(len(scene.freqs), complex)
+        t32 = np.stack([to_transfer(spec32[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
+        t64 = np.stack([to_transfer(spec64[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
+        if scene.weights:
+            w = np.array(scene.weights)  # [nf, S]
+            t32 = np.einsum("fs,srf->rf", w, t32)
+            t64 = np.einsum("fs,srf->rf", w, t64)
+        cent = [c for c in W.OCTAVES if c <= scene.crossover]
+        l32 = W.octave_levels(t32, scene.freqs, cent)
+        l64 = W.octave_levels(t64, scene.freqs, cent)
+        acc = {"octave_band_max_abs_db": float(np.abs(l32 - l64).max()),
+               "octave_bands_hz": cent,
+               "spectra_worst_rel": float(np.abs(spec32 - spec64).max() / np.abs(spec64).max()),
+               "reference": "FP64 GPU run of the same grid (WAVEY_FP64)"}
+
+    # CPU baseline (rank 0 at N = 1): the oracle on a bounded sample.
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import build as obuild
+
+        obuild.build()
+        v, dt, cores = cpu_sample(scene, args.sample_steps)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"1 right-hand side, first {args.sample_steps} steps, all receivers and bins, FP64, "
+                         f"{dt:.1f} s"}
+
+    kernels_per_run = info["graph_kernels"] * (scene.steps // 128) + (scene.steps % 128 + 2 if scene.steps % 128 else 0)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": scene.name, "grid": list(g.n), "air_cells": g.air, "time_steps": scene.steps,
+                       "right_hand_sides": S, "receivers": len(scene.receivers), "freq_bins": len(scene.freqs),
+                       "batched": True, "l2": "fields 2x%.0f MB > L2 (no flush needed)" % (info["device_bytes"] / 2e6),
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "per_source": value / S,
+            "plain": {"value": plain, "per_source": None if plain is None else plain / S,
+                      "batched_over_plain": None if plain is None else value / world / plain},
+            "hbm_gbs": achieved,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "fdtd_step<float,4>", "bytes_per_launch": alg_bytes,
+                         "mean_launch_us": launch_s * 1e6},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": info["h2d_bytes"],
+                    "d2h_bytes_per_step": info["d2h_bytes"], "seconds": e2e_s},
+            "accuracy": acc,
+            "cpu_baseline": cpu,
+            "gpu_launches": int(kernels_per_run * args.steps),
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    plan.close()
+    b.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="room_pillars")
+    ap.add_argument("--sample-steps", type=int, default=120)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warm-up raised to 3 (timing rule)")
+        args.warmup = 3
+    rank, world = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

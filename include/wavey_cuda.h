@@ -1,0 +1,132 @@
+/*
+ * wavey_cuda.h -- C-ABI of libwavey_cuda.so, the GB300 (sm_103a) backend of
+ * Wavey's FDTD wave solver.
+ *
+ * It replaces the wgpu backend `Gpu::run_fdtd` (core/wavey-solver/src/
+ * gpu_fdtd.rs:45-277, shaders core/wavey-solver/src/fdtd.wgsl:44-135) behind
+ * the same contract as its CPU twin `fdtd::run_cpu` (core/wavey-solver/src/
+ * fdtd.rs:616-626) and the `GridRunner` type (fdtd.rs:884-885):
+ *
+ *     (grid, source taps, signal, receiver cells, freqs) -> spectra
+ *
+ * with spectra receiver-major, [receiver][freq] complex.  The scheme, grid
+ * and Courant conventions are the reference's: p^n is recorded before the
+ * update, the update overwrites the older buffer in place, taps are added
+ * after the update, lambda = 1/sqrt(3).
+ *
+ * Status codes are those of wavey_status.h: WAVEY_OK, WAVEY_CANCELLED (the
+ * reference's Ok(None)), or a negative code (the reference's Err(String));
+ * the message is available from wavey_cuda_last_error().  There is no CPU
+ * fallback: a missing or failing device is an error.
+ *
+ * Threading: a context serialises its calls with a mutex; use one context
+ * per thread for concurrent runs.  All host buffers are borrowed for the
+ * duration of a call and never retained.
+ */
+#ifndef WAVEY_CUDA_H
+#define WAVEY_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "wavey_status.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct wavey_cuda_ctx wavey_cuda_ctx;
+typedef struct wavey_cuda_plan wavey_cuda_plan;
+
+/* The voxelised room, `FdtdGrid` (fdtd.rs:196-209) with its boundary nodes
+ * flattened to CSR exactly as the reference packs them for the GPU
+ * (gpu_fdtd.rs:82-88), but in FP64. */
+typedef struct {
+    int64_t nx, ny, nz;        /* cells per axis, x fastest: (z*ny + y)*nx + x */
+    double dx, dt;             /* spacing (m) and time step (s) */
+    const uint8_t *flags;      /* [cells] bit 6 air, bits 0-5 air neighbour -x,+x,-y,+y,-z,+z */
+    const uint32_t *bidx;      /* [cells] boundary node index or 0xFFFFFFFF */
+    int64_t n_boundary;
+    const uint32_t *bstart;    /* [n_boundary + 1] slot range of each boundary node */
+    const double *slots;       /* [bstart[n_boundary]][4] = inv_d, cv, k, w */
+} wavey_grid;
+
+/* A source tap (usize, f64). */
+typedef struct {
+    int64_t cell;
+    double w;
+} wavey_tap;
+
+/* One right-hand side of a batched run: a source component's taps. */
+typedef struct {
+    const wavey_tap *taps;
+    size_t n_taps;
+} wavey_source;
+
+/* Storage precision of the fields. */
+#define WAVEY_FP32 0          /* FP32 throughout, the reference GPU's arithmetic order */
+#define WAVEY_FP64 1          /* FP64 throughout, the reference CPU's order: the GPU oracle */
+
+/* Per-run timing, filled when a stats pointer is given (the run then waits
+ * for each 128-step chunk to read its events). */
+typedef struct {
+    double total_ms;          /* whole run on the device stream */
+    double step_ms;           /* summed span of the fused step launches */
+    int64_t step_launches;
+    int64_t chunks;
+} wavey_run_stats;
+
+typedef struct {
+    int64_t cells, air_cells, interior_cells, special_cells, boundary_slots;
+    int64_t sources, lanes, chunks;       /* lanes per cell in a chunk: 1, 2 or 4 */
+    int64_t receivers, freqs, steps;
+    int64_t device_bytes;                 /* device memory held by the plan */
+    int64_t padded_nx;
+    int32_t precision;
+    int64_t h2d_bytes;                    /* host-to-device bytes of plan_create */
+    int64_t d2h_bytes;                    /* device-to-host bytes of plan_read */
+    int64_t graph_kernels;                /* kernels per replay of the 128-step graph */
+} wavey_plan_info;
+
+int wavey_cuda_create(int device, wavey_cuda_ctx **out);
+void wavey_cuda_destroy(wavey_cuda_ctx *ctx);
+const char *wavey_cuda_last_error(const wavey_cuda_ctx *ctx);
+/* Name and SM count of the context's device. */
+int wavey_cuda_device_info(wavey_cuda_ctx *ctx, char *name, size_t name_cap, int *sm_count);
+
+/* Gpu::run_fdtd (gpu_fdtd.rs:45-54): one source, FP32.  out is
+ * [n_recv][nf][2] (re, im); ir_out (nullable) receives the time series
+ * [n_recv][steps] that `run_cpu_ir` (fdtd.rs:630-641) records.  cancel
+ * (nullable) is polled and progress (nullable) called once per 128 steps. */
+int wavey_cuda_fdtd_run(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_tap *taps, size_t n_taps,
+                        const double *signal, size_t steps, const uint64_t *receivers, size_t n_recv,
+                        const double *freqs, size_t nf, double *out, double *ir_out, const volatile int32_t *cancel,
+                        void (*progress)(double, void *), void *user);
+
+/* S right-hand sides on one grid in one launch per step (source-interleaved
+ * fields).  signals is [S][signal_stride] with signal_stride >= steps, or a
+ * single signal shared by every source when signal_stride == 0.  out is
+ * [S][n_recv][nf][2]; ir_out (nullable) is [S][n_recv][steps]. */
+int wavey_cuda_fdtd_run_batch(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source *sources,
+                              size_t n_sources, const double *signals, size_t signal_stride, size_t steps,
+                              const uint64_t *receivers, size_t n_recv, const double *freqs, size_t nf,
+                              int32_t precision, double *out, double *ir_out, const volatile int32_t *cancel,
+                              void (*progress)(double, void *), void *user);
+
+/* Device-resident form of wavey_cuda_fdtd_run_batch: plan_create uploads
+ * and packs the inputs, plan_run runs (repeatable; each run starts from rest),
+ * plan_read copies the last run's results to the host. */
+int wavey_cuda_plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source *sources, size_t n_sources,
+                           const double *signals, size_t signal_stride, size_t steps, const uint64_t *receivers,
+                           size_t n_recv, const double *freqs, size_t nf, int32_t precision, int32_t want_ir,
+                           wavey_cuda_plan **out);
+int wavey_cuda_plan_run(wavey_cuda_plan *plan, const volatile int32_t *cancel, void (*progress)(double, void *),
+                        void *user, wavey_run_stats *stats);
+int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out);
+int wavey_cuda_plan_info(const wavey_cuda_plan *plan, wavey_plan_info *info);
+void wavey_cuda_plan_destroy(wavey_cuda_plan *plan);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,220 @@
+"""The CUDA backend: the Python face of libwavey_cuda.so.
+
+`CudaBackend.run_fdtd` keeps the contract of the reference's
+`Gpu::run_fdtd` (wavey-solver/src/gpu_fdtd.rs:45-54) and of the CPU twin
+`fdtd::run_cpu` (fdtd.rs:616-626):
+
+    run_fdtd(grid, source_taps, signal, receivers, freqs, cancel, progress)
+        -> spectra [n_recv, nf] complex, or None when cancelled
+
+Limit and device failures raise `WaveyError` (the reference's Err(String)).
+There is no CPU fallback.  `run_batch` advances several right-hand sides
+(speakers x directional components) in one launch per step; `Plan` keeps a
+run resident on the device for repeated timing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+import numpy as np
+
+from . import _native as N
+
+FP32 = N.WAVEY_FP32
+FP64 = N.WAVEY_FP64
+
+
+class WaveyError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{msg} (status {code})")
+        self.code = code
+
+
+def _grid_struct(g):
+    """WaveyGrid over the arrays of an FdtdGrid (or anything with the same
+    attributes: n, dx, dt, flags, bidx, bstart, slots)."""
+    flags = np.ascontiguousarray(g.flags, dtype=np.uint8)
+    bidx = np.ascontiguousarray(g.bidx, dtype=np.uint32)
+    bstart = np.ascontiguousarray(g.bstart, dtype=np.uint32)
+    slots = np.ascontiguousarray(g.slots, dtype=np.float64).reshape(-1)
+    nb = len(bstart) - 1
+    s = N.WaveyGrid(g.n[0], g.n[1], g.n[2], g.dx, g.dt, N.ptr(flags, C.c_uint8), N.ptr(bidx, C.c_uint32), nb,
+                    N.ptr(bstart, C.c_uint32), N.ptr(slots, C.c_double))
+    return s, (flags, bidx, bstart, slots)
+
+
+def _sources_struct(sources):
+    keep = []
+    arr = (N.WaveySource * len(sources))()
+    for i, taps in enumerate(sources):
+        t = (N.WaveyTap * max(len(taps), 1))(*[N.WaveyTap(int(c), float(w)) for c, w in taps])
+        keep.append(t)
+        arr[i].taps = C.cast(t, C.POINTER(N.WaveyTap))
+        arr[i].n_taps = len(taps)
+    return arr, keep
+
+
+def _signals(signal, n_sources: int, steps: int):
+    s = np.asarray(signal, dtype=np.float64)
+    if s.ndim == 1:
+        return np.ascontiguousarray(s), 0
+    if s.shape[0] != n_sources or s.shape[1] < steps:
+        raise ValueError("signals must be [n_sources, steps]")
+    s = np.ascontiguousarray(s)
+    return s, s.shape[1]
+
+
+def _callbacks(cancel, progress):
+    flag = None
+    if cancel is not None:
+        flag = cancel if isinstance(cancel, CancelFlag) else None
+        if flag is None:
+            raise TypeError("cancel must be a CancelFlag")
+    cb = N.PROGRESS_FN(lambda f, _u: progress(f)) if progress is not None else N.PROGRESS_FN()
+    return (C.cast(C.byref(flag._v), C.POINTER(C.c_int32)) if flag else None), cb
+
+
+class CancelFlag:
+    """The reference's `&AtomicBool`: set() from any thread cancels a run at
+    its next 128-step boundary."""
+
+    def __init__(self):
+        self._v = C.c_int32(0)
+
+    def set(self):
+        self._v.value = 1
+
+    def clear(self):
+        self._v.value = 0
+
+    def is_set(self) -> bool:
+        return bool(self._v.value)
+
+
+class CudaBackend:
+    """One device context (libwavey_cuda's wavey_cuda_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = N.cuda()
+        h = C.c_void_p()
+        st = self._lib.wavey_cuda_create(int(device), C.byref(h))
+        if st != 0:
+            raise WaveyError(st, f"no usable CUDA device {device}")
+        self._h = h
+        self._lock = threading.Lock()
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.wavey_cuda_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, st: int):
+        if st < 0:
+            raise WaveyError(st, self._lib.wavey_cuda_last_error(self._h).decode())
+        return st
+
+    def device_info(self):
+        name = C.create_string_buffer(256)
+        sms = C.c_int()
+        self._lib.wavey_cuda_device_info(self._h, name, 256, C.byref(sms))
+        return name.value.decode(), sms.value
+
+    # ---------------------------------------------------------------- runs
+    def run_fdtd(self, grid, source, signal, receivers, freqs, cancel=None, progress=None, ir: bool = False):
+        """Gpu::run_fdtd: spectra [n_recv, nf] (and the time series
+        [n_recv, steps] when ir=True), or None when cancelled."""
+        res = self.run_batch(grid, [source], signal, receivers, freqs, FP32, cancel, progress, ir)
+        if res is None:
+            return None
+        if ir:
+            return res[0][0], res[1][0]
+        return res[0]
+
+    def run_batch(self, grid, sources, signal, receivers, freqs, precision=FP32, cancel=None, progress=None,
+                  ir: bool = False):
+        """S right-hand sides: spectra [S, n_recv, nf] (and ir [S, n_recv,
+        steps]), or None when cancelled.  signal is one shared signal or
+        [S, steps]."""
+        g, keep_g = _grid_struct(grid)
+        srcs, keep_s = _sources_struct(sources)
+        steps = (np.asarray(signal).shape[-1])
+        sig, stride = _signals(signal, len(sources), steps)
+        rx = np.ascontiguousarray(receivers, dtype=np.uint64)
+        fr = np.ascontiguousarray(freqs, dtype=np.float64)
+        S, R, F = len(sources), len(rx), len(fr)
+        out = np.zeros((S, R, F), dtype=np.complex128)
+        irbuf = np.zeros((S, R, steps), dtype=np.float64) if ir else None
+        cflag, cb = _callbacks(cancel, progress)
+        with self._lock:
+            st = self._lib.wavey_cuda_fdtd_run_batch(
+                self._h, C.byref(g), srcs, S, N.ptr(sig, C.c_double), stride, steps, N.ptr(rx, C.c_uint64), R,
+                N.ptr(fr, C.c_double), F, int(precision), N.ptr(out.view(np.float64), C.c_double),
+                N.ptr(irbuf, C.c_double), cflag, cb, None)
+            self._check(st)
+        if st == N.WAVEY_CANCELLED:
+            return None
+        return (out, irbuf) if ir else out
+
+    def plan(self, grid, sources, signal, receivers, freqs, precision=FP32, ir: bool = False) -> "Plan":
+        return Plan(self, grid, sources, signal, receivers, freqs, precision, ir)
+
+
+class Plan:
+    """A run kept on the device: inputs uploaded once, run() repeatable."""
+
+    def __init__(self, backend: CudaBackend, grid, sources, signal, receivers, freqs, precision, ir):
+        self._b = backend
+        g, keep_g = _grid_struct(grid)
+        srcs, keep_s = _sources_struct(sources)
+        steps = np.asarray(signal).shape[-1]
+        sig, stride = _signals(signal, len(sources), steps)
+        rx = np.ascontiguousarray(receivers, dtype=np.uint64)
+        fr = np.ascontiguousarray(freqs, dtype=np.float64)
+        self.shape = (len(sources), len(rx), len(fr))
+        self.steps = steps
+        self.ir = ir
+        h = C.c_void_p()
+        with backend._lock:
+            backend._check(backend._lib.wavey_cuda_plan_create(
+                backend._h, C.byref(g), srcs, len(sources), N.ptr(sig, C.c_double), stride, steps,
+                N.ptr(rx, C.c_uint64), len(rx), N.ptr(fr, C.c_double), len(fr), int(precision), int(ir),
+                C.byref(h)))
+        self._h = h
+
+    def run(self, cancel=None, progress=None, stats: bool = False):
+        cflag, cb = _callbacks(cancel, progress)
+        s = N.WaveyRunStats()
+        with self._b._lock:
+            st = self._b._check(self._b._lib.wavey_cuda_plan_run(self._h, cflag, cb, None,
+                                                                 C.byref(s) if stats else None))
+        if st == N.WAVEY_CANCELLED:
+            return None
+        if stats:
+            return {"total_ms": s.total_ms, "step_ms": s.step_ms, "step_launches": s.step_launches,
+                    "chunks": s.chunks}
+        return True
+
+    def read(self):
+        out = np.zeros(self.shape, dtype=np.complex128)
+        irbuf = np.zeros((self.shape[0], self.shape[1], self.steps)) if self.ir else None
+        with self._b._lock:
+            self._b._check(self._b._lib.wavey_cuda_plan_read(self._h, N.ptr(out.view(np.float64), C.c_double),
+                                                             N.ptr(irbuf, C.c_double)))
+        return (out, irbuf) if self.ir else out
+
+    def info(self) -> dict:
+        i = N.WaveyPlanInfo()
+        self._b._lib.wavey_cuda_plan_info(self._h, C.byref(i))
+        return {k: getattr(i, k) for k, _ in N.WaveyPlanInfo._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._b._lib.wavey_cuda_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()

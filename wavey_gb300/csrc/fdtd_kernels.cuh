@@ -1,0 +1,380 @@
+// fdtd_kernels.cuh -- the FDTD time step on sm_103a.
+//
+// One fused launch per time step.  Its CTAs take one of three roles, all of
+// which read only p^n and write disjoint cells of the older buffer, so they
+// need no ordering among themselves:
+//
+//   interior  the leapfrog update of plain air cells (six air neighbours, no
+//             boundary slot, no source tap), selected by a one-bit-per-cell
+//             mask.  A warp owns 32 consecutive x cells of one row and marches
+//             a run of z planes, keeping p(z-1), p(z), p(z+1) in registers.
+//             Reference: fdtd.rs:697-708 (CPU), fdtd.wgsl:50-62 (GPU).
+//   special   every other air cell, from a compacted list sorted by cell:
+//             cells with rigid faces (K < 6 air neighbours, fdtd.wgsl:64-81),
+//             boundary nodes with admittance slots solved jointly with their
+//             branch states (boundary_update, fdtd.rs:580-598, fdtd.wgsl:
+//             83-104), and source taps, whose injection (fdtd.rs:718-720,
+//             fdtd.wgsl:110-119) is fused as the last operation of the update.
+//   record    copies p^n at every receiver into a ring buffer of RING steps
+//             (the samples of fdtd.rs:674-683, taken before the update).
+//
+// Every 128 steps a twiddle kernel and a DFT kernel fold the ring into the
+// FP64 receiver spectra; see dft_chunk below.
+//
+// Fields are source-interleaved: a chunk of V right-hand sides (V = 1, 2 or
+// 4) stores the V values of a cell contiguously, so one 128-bit access
+// carries four sources in FP32.  Rows are padded to a multiple of 32 cells
+// (128 bytes per lane), so every warp row access is aligned and a warp's
+// interior mask is one 32-bit word.
+//
+// Arithmetic: every product, sum and quotient is rounded separately, in the
+// order of the reference (WGSL order for FP32, the CPU's Rust order for
+// FP64), so that receiver time series match a restatement of the reference
+// bit for bit.  The stencil is memory-bound, so the lost FMA contraction
+// costs nothing.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wk {
+
+constexpr int RING = 128;          // steps per chunk; even, so buffer parity repeats per chunk
+constexpr int BLOCK = 256;         // threads per CTA, every role
+constexpr int TILE_Y = BLOCK / 32; // rows per interior CTA
+constexpr uint32_t NO_TAP = 0xFFFFFFFFu;
+constexpr int META_SLOT_SHIFT = 6;
+constexpr uint32_t META_SLOT_MASK = 31u;
+
+// ------------------------------------------------------------ rounded ops
+__device__ __forceinline__ float radd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float rsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float rmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float rdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double radd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double rsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double rmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double rdiv(double a, double b) { return __ddiv_rn(a, b); }
+
+// -------------------------------------------------------- lane vectors
+template <class T, int V>
+struct Lanes {
+    T v[V];
+};
+
+// Loads of the current field go through the read-only path (p^n is never
+// written during a step); the older buffer is read and written.
+template <class T, int V, bool RO>
+__device__ __forceinline__ Lanes<T, V> load(const T *p) {
+    Lanes<T, V> o;
+    if constexpr (sizeof(T) * V == 16) {
+        if constexpr (sizeof(T) == 4) {
+            float4 x = RO ? __ldg(reinterpret_cast<const float4 *>(p)) : *reinterpret_cast<const float4 *>(p);
+            o.v[0] = x.x; o.v[1] = x.y; o.v[2] = x.z; o.v[3] = x.w;
+        } else {
+            double2 x = RO ? __ldg(reinterpret_cast<const double2 *>(p)) : *reinterpret_cast<const double2 *>(p);
+            o.v[0] = x.x; o.v[1] = x.y;
+        }
+    } else if constexpr (sizeof(T) * V == 8 && sizeof(T) == 4) {
+        float2 x = RO ? __ldg(reinterpret_cast<const float2 *>(p)) : *reinterpret_cast<const float2 *>(p);
+        o.v[0] = x.x; o.v[1] = x.y;
+    } else if constexpr (sizeof(T) * V == 32) {
+        double2 a = RO ? __ldg(reinterpret_cast<const double2 *>(p)) : *reinterpret_cast<const double2 *>(p);
+        double2 b = RO ? __ldg(reinterpret_cast<const double2 *>(p) + 1) : *(reinterpret_cast<const double2 *>(p) + 1);
+        o.v[0] = a.x; o.v[1] = a.y; o.v[2] = b.x; o.v[3] = b.y;
+    } else {
+#pragma unroll
+        for (int l = 0; l < V; l++) o.v[l] = RO ? __ldg(p + l) : p[l];
+    }
+    return o;
+}
+
+template <class T, int V>
+__device__ __forceinline__ void store(T *p, const Lanes<T, V> &o) {
+    if constexpr (sizeof(T) * V == 16) {
+        if constexpr (sizeof(T) == 4) {
+            *reinterpret_cast<float4 *>(p) = make_float4(o.v[0], o.v[1], o.v[2], o.v[3]);
+        } else {
+            *reinterpret_cast<double2 *>(p) = make_double2(o.v[0], o.v[1]);
+        }
+    } else if constexpr (sizeof(T) * V == 8 && sizeof(T) == 4) {
+        *reinterpret_cast<float2 *>(p) = make_float2(o.v[0], o.v[1]);
+    } else if constexpr (sizeof(T) * V == 32) {
+        reinterpret_cast<double2 *>(p)[0] = make_double2(o.v[0], o.v[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(o.v[2], o.v[3]);
+    } else {
+#pragma unroll
+        for (int l = 0; l < V; l++) p[l] = o.v[l];
+    }
+}
+
+// ------------------------------------------------------------ arguments
+template <class T>
+struct StepArgs {
+    const T *cur;              // p^n        [chunks][cells_p][V]
+    T *nxt;                    // p^{n-1} in, p^{n+1} out
+    const uint32_t *interior;  // [nz][ny][nxw] one bit per padded cell
+    const uint32_t *sp_cell;   // [n_special] padded cell index, ascending
+    const uint32_t *sp_meta;   // bits 0-5 air-neighbour flags, bits 6-10 slot count
+    const uint32_t *sp_slot0;  // first slot of the node
+    const uint32_t *sp_tap;    // tap row or NO_TAP
+    const T *slots;            // [n_slots][4] inv_d, cv, k, w
+    T *su, *sg;                // [chunks][n_slots][V] branch velocity u and its integral g
+    const T *tapw;             // [n_tap_rows][lanes_total] merged tap weight per source
+    const T *sig;              // [lanes_total][sig_stride] or one shared row (sig_stride 0)
+    const uint32_t *recv;      // [n_recv] padded receiver cells
+    T *ring;                   // [chunks][RING][n_recv][V]
+    const long long *base;     // step index of the chunk's first step
+    long long cells_p;         // padded cells per chunk
+    long long sig_stride;
+    int nxp, ny, nz, nxw;
+    int n_special, n_slots, n_recv, chunks, lanes_total;
+    int tiles_x, tiles_y, tiles_z, zt;
+    int interior_blocks, special_blocks, record_blocks;
+    T l2, lam, half_dt;
+};
+
+// The interior update of one cell, WGSL order (fdtd.wgsl:52-61), which is
+// also the CPU order (fdtd.rs:706 with lap of fdtd.rs:685-696 and K = 6).
+template <class T, int V>
+__device__ __forceinline__ Lanes<T, V> interior_update(const Lanes<T, V> &c, const Lanes<T, V> &old, const Lanes<T, V> &xm,
+                                                       const Lanes<T, V> &xp, const Lanes<T, V> &ym, const Lanes<T, V> &yp,
+                                                       const Lanes<T, V> &zm, const Lanes<T, V> &zp, T l2) {
+    Lanes<T, V> o;
+#pragma unroll
+    for (int l = 0; l < V; l++) {
+        T s = radd(xm.v[l], xp.v[l]);
+        s = radd(s, ym.v[l]);
+        s = radd(s, yp.v[l]);
+        s = radd(s, zm.v[l]);
+        s = radd(s, zp.v[l]);
+        T six = T(6);
+        T two = T(2);
+        o.v[l] = radd(rsub(rmul(two, c.v[l]), old.v[l]), rmul(l2, rsub(s, rmul(six, c.v[l]))));
+    }
+    return o;
+}
+
+// ------------------------------------------------------------------ step
+// RUST_ORDER selects the CPU reference's association of the branch sum
+// (s2 + (e - u), fdtd.rs:588) instead of the shader's ((s2 + e) - u,
+// fdtd.wgsl:94).
+template <class T, int V, bool RUST_ORDER>
+__global__ void __launch_bounds__(BLOCK) fdtd_step(StepArgs<T> a, int t) {
+    int b = blockIdx.x;
+    const long long nxy = (long long)a.nxp * a.ny;
+    if (b < a.interior_blocks) {
+        // ---------------------------------------------------- interior
+        const int per_chunk = a.tiles_x * a.tiles_y * a.tiles_z;
+        const int c = b / per_chunk;
+        int r = b - c * per_chunk;
+        const int tz = r / (a.tiles_x * a.tiles_y);
+        r -= tz * a.tiles_x * a.tiles_y;
+        const int ty = r / a.tiles_x;
+        const int tx = r - ty * a.tiles_x;
+        const int lane = threadIdx.x & 31;
+        const int y = 1 + ty * TILE_Y + (threadIdx.x >> 5);
+        if (y >= a.ny - 1) return;
+        const int x = tx * 32 + lane;
+        const int zs = 1 + tz * a.zt;
+        const int ze = min(zs + a.zt, a.nz - 1);
+        const T *P = a.cur + (long long)c * a.cells_p * V;
+        T *Q = a.nxt + (long long)c * a.cells_p * V;
+        long long i = ((long long)zs * a.ny + y) * a.nxp + x;
+        const uint32_t *mrow = a.interior + ((long long)zs * a.ny + y) * a.nxw + tx;
+        const long long mstep = (long long)a.ny * a.nxw;
+        Lanes<T, V> zm, zc, zp;
+        bool have = false;
+        for (int z = zs; z < ze; ++z, i += nxy, mrow += mstep) {
+            const uint32_t word = __ldg(mrow);
+            if (word == 0u) {  // uniform per warp: a solid or special-only row segment
+                have = false;
+                continue;
+            }
+            if (!have) {
+                zm = load<T, V, true>(P + (i - nxy) * V);
+                zc = load<T, V, true>(P + i * V);
+                have = true;
+            }
+            zp = load<T, V, true>(P + (i + nxy) * V);
+            if ((word >> lane) & 1u) {
+                Lanes<T, V> xm = load<T, V, true>(P + (i - 1) * V);
+                Lanes<T, V> xp = load<T, V, true>(P + (i + 1) * V);
+                Lanes<T, V> ym = load<T, V, true>(P + (i - a.nxp) * V);
+                Lanes<T, V> yp = load<T, V, true>(P + (i + a.nxp) * V);
+                Lanes<T, V> old = load<T, V, false>(Q + i * V);
+                store<T, V>(Q + i * V, interior_update<T, V>(zc, old, xm, xp, ym, yp, zm, zp, a.l2));
+            }
+            zm = zc;
+            zc = zp;
+        }
+        return;
+    }
+    b -= a.interior_blocks;
+    const long long n = *a.base + t;
+    if (b < a.special_blocks) {
+        // ----------------------------------------------------- special
+        long long k = (long long)b * BLOCK + threadIdx.x;
+        if (k >= (long long)a.n_special * a.chunks) return;
+        const int c = (int)(k / a.n_special);
+        k -= (long long)c * a.n_special;
+        const long long cell = a.sp_cell[k];
+        const uint32_t m = a.sp_meta[k];
+        const T *P = a.cur + (long long)c * a.cells_p * V;
+        T *Q = a.nxt + (long long)c * a.cells_p * V;
+        const Lanes<T, V> pc = load<T, V, true>(P + cell * V);
+        const Lanes<T, V> pp = load<T, V, false>(Q + cell * V);
+        const long long offs[6] = {-1, 1, -(long long)a.nxp, (long long)a.nxp, -nxy, nxy};
+        Lanes<T, V> sum;
+#pragma unroll
+        for (int l = 0; l < V; l++) sum.v[l] = T(0);
+        T kk = T(0);
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if ((m >> d) & 1u) {
+                Lanes<T, V> nb = load<T, V, true>(P + (cell + offs[d]) * V);
+#pragma unroll
+                for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb.v[l]);
+                kk = radd(kk, T(1));
+            }
+        }
+        Lanes<T, V> lap, next;
+#pragma unroll
+        for (int l = 0; l < V; l++) lap.v[l] = rmul(a.l2, rsub(sum.v[l], rmul(kk, pc.v[l])));
+        const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
+        const T half = T(0.5), two = T(2), one = T(1);
+        if (ns == 0) {
+#pragma unroll
+            for (int l = 0; l < V; l++) next.v[l] = radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]);
+        } else {
+            const long long j0 = a.sp_slot0[k];
+            T *SU = a.su + (long long)c * a.n_slots * V;
+            T *SG = a.sg + (long long)c * a.n_slots * V;
+            T s1 = T(0);
+            Lanes<T, V> s2;
+#pragma unroll
+            for (int l = 0; l < V; l++) s2.v[l] = T(0);
+            for (int q = 0; q < ns; q++) {
+                const long long j = j0 + q;
+                const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
+                const Lanes<T, V> u = load<T, V, false>(SU + j * V);
+                const Lanes<T, V> g = load<T, V, false>(SG + j * V);
+#pragma unroll
+                for (int l = 0; l < V; l++) {
+                    T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
+                    s2.v[l] = RUST_ORDER ? radd(s2.v[l], rsub(e, u.v[l])) : rsub(radd(s2.v[l], e), u.v[l]);
+                }
+                s1 = radd(s1, rmul(rsub(half, w), inv_d));
+            }
+            const T den = radd(one, rmul(a.lam, s1));
+#pragma unroll
+            for (int l = 0; l < V; l++)
+                next.v[l] = rdiv(rsub(radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]), rmul(a.lam, s2.v[l])), den);
+            for (int q = 0; q < ns; q++) {
+                const long long j = j0 + q;
+                const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
+                Lanes<T, V> u = load<T, V, false>(SU + j * V);
+                Lanes<T, V> g = load<T, V, false>(SG + j * V);
+#pragma unroll
+                for (int l = 0; l < V; l++) {
+                    T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
+                    T un = radd(rmul(rmul(rsub(half, w), inv_d), next.v[l]), e);
+                    g.v[l] = radd(g.v[l], rmul(a.half_dt, radd(un, u.v[l])));
+                    u.v[l] = un;
+                }
+                store<T, V>(SU + j * V, u);
+                store<T, V>(SG + j * V, g);
+            }
+        }
+        const uint32_t tap = a.sp_tap[k];
+        if (tap != NO_TAP) {
+#pragma unroll
+            for (int l = 0; l < V; l++) {
+                const int s = c * V + l;
+                const T sv = a.sig[(long long)s * a.sig_stride + n];
+                next.v[l] = radd(next.v[l], rmul(sv, a.tapw[(long long)tap * a.lanes_total + s]));
+            }
+        }
+        store<T, V>(Q + cell * V, next);
+        return;
+    }
+    b -= a.special_blocks;
+    // --------------------------------------------------------- record
+    long long k = (long long)b * BLOCK + threadIdx.x;
+    if (k >= (long long)a.n_recv * a.chunks) return;
+    const int c = (int)(k / a.n_recv);
+    const long long r = k - (long long)c * a.n_recv;
+    const T *P = a.cur + (long long)c * a.cells_p * V;
+    const Lanes<T, V> v = load<T, V, true>(P + (long long)a.recv[r] * V);
+    store<T, V>(a.ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
+}
+
+// ------------------------------------------------------------- twiddles
+// tw[t][f] = exp(-j 2 pi frac(f dt n)) for n = base + t, phase in FP64
+// exactly as fdtd.rs:680 forms it.
+template <class T>
+__global__ void twiddle_chunk(const double *freqs, int nf, double dt, const long long *base, int count, T *tw) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= count * nf) return;
+    const int t = idx / nf, f = idx - t * nf;
+    const double x = freqs[f] * dt * (double)(*base + t);
+    const double ph = -6.283185307179586 * (x - trunc(x));
+    double s, c;
+    sincos(ph, &s, &c);
+    tw[2 * idx] = (T)c;
+    tw[2 * idx + 1] = (T)s;
+}
+
+// ------------------------------------------------------------------ DFT
+// acc[c][r][f][l] += sum_t ring[c][t][r][l] * tw[t][f], the partial sum of a
+// chunk in T, added into FP64.  One thread per (chunk, receiver, freq).
+template <class T, int V>
+__global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const T *tw, double *acc, int n_recv, int nf, int chunks,
+                                                   int count) {
+    const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    const long long total = (long long)chunks * n_recv * nf;
+    if (idx >= total) return;
+    const long long rf = idx % ((long long)n_recv * nf);
+    const int c = (int)(idx / ((long long)n_recv * nf));
+    const int r = (int)(rf / nf), f = (int)(rf - (long long)r * nf);
+    T re[V], im[V];
+#pragma unroll
+    for (int l = 0; l < V; l++) re[l] = im[l] = T(0);
+    const T *src = ring + ((long long)c * RING * n_recv + r) * V;
+    for (int t = 0; t < count; t++) {
+        const Lanes<T, V> v = load<T, V, true>(src + (long long)t * n_recv * V);
+        const T wr = __ldg(tw + 2 * (t * nf + f)), wi = __ldg(tw + 2 * (t * nf + f) + 1);
+#pragma unroll
+        for (int l = 0; l < V; l++) {
+            re[l] = fma(v.v[l], wr, re[l]);
+            im[l] = fma(v.v[l], wi, im[l]);
+        }
+    }
+    double *out = acc + idx * V * 2;
+#pragma unroll
+    for (int l = 0; l < V; l++) {
+        out[2 * l] += (double)re[l];
+        out[2 * l + 1] += (double)im[l];
+    }
+}
+
+// ir[s][r][n0 + t] = ring[c][t][r][l] (s = c*V + l): the time series of
+// run_cpu_ir (fdtd.rs:628-641).
+template <class T, int V>
+__global__ void ir_chunk(const T *ring, T *ir, int n_recv, int chunks, int n_sources, long long steps,
+                         const long long *base, int count) {
+    const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    const long long total = (long long)chunks * V * n_recv * count;
+    if (idx >= total) return;
+    const int t = (int)(idx % count);
+    long long rest = idx / count;
+    const int r = (int)(rest % n_recv);
+    rest /= n_recv;
+    const int s = (int)rest;  // c * V + l
+    if (s >= n_sources) return;
+    const int c = s / V, l = s - c * V;
+    ir[((long long)s * n_recv + r) * steps + *base + t] = ring[(((long long)c * RING + t) * n_recv + r) * V + l];
+}
+
+__global__ void advance_base(long long *base, int by) { *base += by; }
+
+}  // namespace wk

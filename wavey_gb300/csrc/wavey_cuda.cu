@@ -1,0 +1,782 @@
+// wavey_cuda.cu -- libwavey_cuda.so: the C-ABI backend that replaces
+// `Gpu::run_fdtd` (core/wavey-solver/src/gpu_fdtd.rs:45-277).
+//
+// Host side of a run:
+//   1. validate the grid, taps and receivers (the reference's limit checks,
+//      gpu_fdtd.rs:56-66, become error codes; indices are checked here so no
+//      kernel ever sees an out-of-range cell);
+//   2. pack: the interior mask and the compacted special-cell list on the
+//      padded device layout, slot constants, merged taps (gpu_fdtd.rs:67-75),
+//      signals and receivers, in the run's precision;
+//   3. capture one 128-step chunk (128 fused step launches, the chunk's
+//      twiddles and DFT, the optional time-series copy, and the step-counter
+//      advance) into a CUDA graph, and replay it steps/128 times; the
+//      remaining steps are launched directly;
+//   4. read the FP64 spectra (and time series) back.
+// The reference's blocking poll per 128-step submit (gpu_fdtd.rs:254-259)
+// becomes an event wait only when a cancel flag, a progress callback or
+// statistics are requested.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/wavey_cuda.h"
+#include "fdtd_kernels.cuh"
+
+namespace {
+
+constexpr double COURANT = 0.5773502691896257;  // fdtd.rs:138
+constexpr uint64_t MAX_CELLS = 600000000ull;      // fdtd.rs:140
+constexpr uint32_t NO_BOUNDARY = 0xFFFFFFFFu;
+constexpr uint8_t AIR = 64;
+constexpr int ZT = 16;  // z planes marched by one interior CTA
+
+struct Status {
+    int code;
+    std::string msg;
+};
+
+}  // namespace
+
+struct wavey_cuda_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::string err;
+    char name[256] = {0};
+
+    int fail(int code, const char *fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda(cudaError_t e, const char *what) {
+        if (e == cudaSuccess) return WAVEY_OK;
+        return fail(e == cudaErrorMemoryAllocation ? WAVEY_E_NOMEM : WAVEY_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct wavey_cuda_plan {
+    wavey_cuda_ctx *ctx = nullptr;
+    int precision = WAVEY_FP32;
+    int V = 1;
+    int chunks = 1;
+    int n_sources = 0;
+    int lanes_total = 0;
+    int64_t nx = 0, ny = 0, nz = 0, nxp = 0, cells = 0, cells_p = 0;
+    int64_t air = 0, interior = 0, n_special = 0, n_slots = 0;
+    int64_t steps = 0, n_recv = 0, nf = 0;
+    bool want_ir = false;
+    double dt = 0.0;
+    std::vector<DevBuf> bufs;
+    // device pointers
+    void *field[2] = {nullptr, nullptr};
+    uint32_t *mask = nullptr, *sp_cell = nullptr, *sp_meta = nullptr, *sp_slot0 = nullptr, *sp_tap = nullptr, *recv = nullptr;
+    void *slots = nullptr, *su = nullptr, *sg = nullptr, *tapw = nullptr, *sig = nullptr, *ring = nullptr, *tw = nullptr,
+         *ir = nullptr;
+    double *acc = nullptr, *freqs = nullptr;
+    long long *base = nullptr;
+    int64_t sig_stride = 0;
+    size_t field_bytes = 0, state_bytes = 0, acc_bytes = 0, ir_bytes = 0, elem = 4;
+    // launch geometry
+    int tiles_x = 0, tiles_y = 0, tiles_z = 0;
+    int interior_blocks = 0, special_blocks = 0, record_blocks = 0;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_kernels = 0;  // kernel launches per replay of the chunk graph
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
+    cudaEvent_t inflight[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool ran = false;
+    int64_t device_bytes = 0;
+    int64_t h2d_bytes = 0;  // bytes uploaded by plan_create
+
+    ~wavey_cuda_plan() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1, inflight[0], inflight[1], inflight[2], inflight[3]})
+            if (e) cudaEventDestroy(e);
+        for (DevBuf &b : bufs)
+            if (b.p) cudaFree(b.p);
+    }
+};
+
+namespace {
+
+template <class T>
+int alloc(wavey_cuda_plan *pl, T **out, size_t bytes) {
+    void *p = nullptr;
+    size_t b = std::max<size_t>(bytes, 16);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return pl->ctx->fail(WAVEY_E_NOMEM, "device allocation of %zu bytes failed: %s", b, cudaGetErrorString(e));
+    }
+    pl->bufs.push_back({p, b});
+    pl->device_bytes += (int64_t)b;
+    *out = reinterpret_cast<T *>(p);
+    return WAVEY_OK;
+}
+
+template <class T>
+int upload(wavey_cuda_plan *pl, T **out, const void *host, size_t bytes) {
+    int st = alloc(pl, out, bytes);
+    if (st) return st;
+    pl->h2d_bytes += (int64_t)bytes;
+    if (bytes) return pl->ctx->cuda(cudaMemcpyAsync(*out, host, bytes, cudaMemcpyHostToDevice, pl->ctx->stream), "upload");
+    return WAVEY_OK;
+}
+
+inline int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+int validate_grid(wavey_cuda_ctx *ctx, const wavey_grid *g) {
+    if (!g) return ctx->fail(WAVEY_E_INVALID, "grid is null");
+    if (g->nx < 3 || g->ny < 3 || g->nz < 3) return ctx->fail(WAVEY_E_INVALID, "grid must be at least 3 cells per axis");
+    const uint64_t cells = (uint64_t)g->nx * (uint64_t)g->ny * (uint64_t)g->nz;
+    if (cells > MAX_CELLS)
+        return ctx->fail(WAVEY_E_LIMIT, "the wave solver grid would have %.0f M cells; lower the crossover frequency",
+                         cells / 1e6);
+    if (!g->flags || !g->bidx) return ctx->fail(WAVEY_E_INVALID, "grid flags/bidx are null");
+    if (!(g->dt > 0.0) || !(g->dx > 0.0)) return ctx->fail(WAVEY_E_INVALID, "grid dx/dt must be positive");
+    if (g->n_boundary < 0 || (g->n_boundary > 0 && (!g->bstart || !g->slots)))
+        return ctx->fail(WAVEY_E_INVALID, "grid boundary arrays are null");
+    if (g->n_boundary >= (1ll << 31)) return ctx->fail(WAVEY_E_LIMIT, "too many boundary nodes");
+    if (g->n_boundary > 0) {
+        if (g->bstart[0] != 0) return ctx->fail(WAVEY_E_INVALID, "bstart[0] must be 0");
+        for (int64_t b = 0; b < g->n_boundary; b++) {
+            if (g->bstart[b + 1] < g->bstart[b]) return ctx->fail(WAVEY_E_INVALID, "bstart is not ascending at %lld", (long long)b);
+            if (g->bstart[b + 1] - g->bstart[b] > wk::META_SLOT_MASK)
+                return ctx->fail(WAVEY_E_LIMIT, "boundary node %lld has more than %u slots", (long long)b, wk::META_SLOT_MASK);
+        }
+    }
+    return WAVEY_OK;
+}
+
+template <class T>
+void fill_args(wavey_cuda_plan *pl, wk::StepArgs<T> &a, int parity) {
+    a.cur = reinterpret_cast<const T *>(pl->field[parity]);
+    a.nxt = reinterpret_cast<T *>(pl->field[parity ^ 1]);
+    a.interior = pl->mask;
+    a.sp_cell = pl->sp_cell;
+    a.sp_meta = pl->sp_meta;
+    a.sp_slot0 = pl->sp_slot0;
+    a.sp_tap = pl->sp_tap;
+    a.slots = reinterpret_cast<const T *>(pl->slots);
+    a.su = reinterpret_cast<T *>(pl->su);
+    a.sg = reinterpret_cast<T *>(pl->sg);
+    a.tapw = reinterpret_cast<const T *>(pl->tapw);
+    a.sig = reinterpret_cast<const T *>(pl->sig);
+    a.recv = pl->recv;
+    a.ring = reinterpret_cast<T *>(pl->ring);
+    a.base = pl->base;
+    a.cells_p = pl->cells_p;
+    a.sig_stride = pl->sig_stride;
+    a.nxp = (int)pl->nxp;
+    a.ny = (int)pl->ny;
+    a.nz = (int)pl->nz;
+    a.nxw = (int)(pl->nxp / 32);
+    a.n_special = (int)pl->n_special;
+    a.n_slots = (int)pl->n_slots;
+    a.n_recv = (int)pl->n_recv;
+    a.chunks = pl->chunks;
+    a.lanes_total = pl->lanes_total;
+    a.tiles_x = pl->tiles_x;
+    a.tiles_y = pl->tiles_y;
+    a.tiles_z = pl->tiles_z;
+    a.zt = ZT;
+    a.interior_blocks = pl->interior_blocks;
+    a.special_blocks = pl->special_blocks;
+    a.record_blocks = pl->record_blocks;
+    a.l2 = (T)(COURANT * COURANT);
+    a.lam = (T)COURANT;
+    a.half_dt = (T)0.5 * (T)pl->dt;
+}
+
+template <class T, int V, bool RUST>
+void launch_step(wavey_cuda_plan *pl, int t, int parity) {
+    wk::StepArgs<T> a;
+    fill_args<T>(pl, a, parity);
+    const int blocks = pl->interior_blocks + pl->special_blocks + pl->record_blocks;
+    if (blocks > 0) wk::fdtd_step<T, V, RUST><<<blocks, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
+}
+
+void step(wavey_cuda_plan *pl, int t, int parity) {
+    if (pl->precision == WAVEY_FP64) {
+        switch (pl->V) {
+            case 1: launch_step<double, 1, true>(pl, t, parity); break;
+            case 2: launch_step<double, 2, true>(pl, t, parity); break;
+            default: launch_step<double, 4, true>(pl, t, parity); break;
+        }
+    } else {
+        switch (pl->V) {
+            case 1: launch_step<float, 1, false>(pl, t, parity); break;
+            case 2: launch_step<float, 2, false>(pl, t, parity); break;
+            default: launch_step<float, 4, false>(pl, t, parity); break;
+        }
+    }
+}
+
+template <class T, int V>
+void launch_fold(wavey_cuda_plan *pl, int count) {
+    cudaStream_t s = pl->ctx->stream;
+    const int tw_threads = count * (int)pl->nf;
+    if (tw_threads > 0)
+        wk::twiddle_chunk<T><<<(tw_threads + 255) / 256, 256, 0, s>>>(pl->freqs, (int)pl->nf, pl->dt, pl->base, count,
+                                                                       reinterpret_cast<T *>(pl->tw));
+    const long long total = (long long)pl->chunks * pl->n_recv * pl->nf;
+    if (total > 0)
+        wk::dft_chunk<T, V><<<(unsigned)((total + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
+            reinterpret_cast<const T *>(pl->ring), reinterpret_cast<const T *>(pl->tw), pl->acc, (int)pl->n_recv, (int)pl->nf,
+            pl->chunks, count);
+    if (pl->want_ir) {
+        const long long n = (long long)pl->chunks * V * pl->n_recv * count;
+        if (n > 0)
+            wk::ir_chunk<T, V><<<(unsigned)((n + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
+                reinterpret_cast<const T *>(pl->ring), reinterpret_cast<T *>(pl->ir), (int)pl->n_recv, pl->chunks,
+                pl->n_sources, (long long)pl->steps, pl->base, count);
+    }
+}
+
+void fold(wavey_cuda_plan *pl, int count) {
+    if (pl->precision == WAVEY_FP64) {
+        switch (pl->V) {
+            case 1: launch_fold<double, 1>(pl, count); break;
+            case 2: launch_fold<double, 2>(pl, count); break;
+            default: launch_fold<double, 4>(pl, count); break;
+        }
+    } else {
+        switch (pl->V) {
+            case 1: launch_fold<float, 1>(pl, count); break;
+            case 2: launch_fold<float, 2>(pl, count); break;
+            default: launch_fold<float, 4>(pl, count); break;
+        }
+    }
+}
+
+int build_graph(wavey_cuda_plan *pl) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    cudaStream_t s = ctx->stream;
+    cudaGraph_t g = nullptr;
+    int st = ctx->cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (st) return st;
+    cudaEventRecordWithFlags(pl->ev_a, s, cudaEventRecordExternal);
+    for (int t = 0; t < wk::RING; t++) step(pl, t, t & 1);
+    cudaEventRecordWithFlags(pl->ev_b, s, cudaEventRecordExternal);
+    fold(pl, wk::RING);
+    wk::advance_base<<<1, 1, 0, s>>>(pl->base, wk::RING);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess) return ctx->cuda(e, "end capture");
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    pl->graph_kernels = (int64_t)nodes - 2;  // minus the two event-record nodes
+    e = cudaGraphInstantiate(&pl->graph, g, 0);
+    cudaGraphDestroy(g);
+    return ctx->cuda(e, "graph instantiate");
+}
+
+template <class T>
+std::vector<T> convert(const double *src, size_t n) {
+    std::vector<T> v(n);
+    for (size_t i = 0; i < n; i++) v[i] = (T)src[i];
+    return v;
+}
+
+template <class T>
+int upload_typed(wavey_cuda_plan *pl, void **out, const std::vector<double> &src) {
+    std::vector<T> v = convert<T>(src.data(), src.size());
+    T *d = nullptr;
+    int st = upload(pl, &d, v.data(), v.size() * sizeof(T));
+    *out = d;
+    if (st) return st;
+    // The staging vector dies here: wait for the copy.
+    return pl->ctx->cuda(cudaStreamSynchronize(pl->ctx->stream), "upload sync");
+}
+
+int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source *sources, size_t n_sources,
+                const double *signals, size_t signal_stride, size_t steps, const uint64_t *receivers, size_t n_recv,
+                const double *freqs, size_t nf, int32_t precision, int32_t want_ir, wavey_cuda_plan **out) {
+    if (!out) return ctx->fail(WAVEY_E_INVALID, "out is null");
+    *out = nullptr;
+    int st = validate_grid(ctx, grid);
+    if (st) return st;
+    if (precision != WAVEY_FP32 && precision != WAVEY_FP64) return ctx->fail(WAVEY_E_INVALID, "unknown precision %d", precision);
+    if (n_sources == 0 || !sources) return ctx->fail(WAVEY_E_INVALID, "no sources");
+    if (n_sources > 4096) return ctx->fail(WAVEY_E_LIMIT, "at most 4096 sources per run");
+    if (steps > 0 && !signals) return ctx->fail(WAVEY_E_INVALID, "signals are null");
+    if (signal_stride != 0 && signal_stride < steps) return ctx->fail(WAVEY_E_INVALID, "signal_stride is shorter than steps");
+    if (steps >= (1ull << 40)) return ctx->fail(WAVEY_E_LIMIT, "too many steps");
+    if (n_recv > 0 && !receivers) return ctx->fail(WAVEY_E_INVALID, "receivers are null");
+    if (nf > 0 && !freqs) return ctx->fail(WAVEY_E_INVALID, "freqs are null");
+    if (n_recv > (1u << 26) || nf > (1u << 20)) return ctx->fail(WAVEY_E_LIMIT, "too many receivers or frequencies");
+
+    const int64_t nx = grid->nx, ny = grid->ny, nz = grid->nz;
+    const int64_t cells = nx * ny * nz;
+    wavey_cuda_plan *pl = new (std::nothrow) wavey_cuda_plan();
+    if (!pl) return ctx->fail(WAVEY_E_NOMEM, "host allocation failed");
+    pl->ctx = ctx;
+    pl->precision = precision;
+    pl->elem = precision == WAVEY_FP64 ? 8 : 4;
+    pl->n_sources = (int)n_sources;
+    pl->V = n_sources >= 4 ? 4 : (n_sources == 1 ? 1 : (n_sources == 2 ? 2 : 4));
+    pl->chunks = (int)((n_sources + pl->V - 1) / pl->V);
+    pl->lanes_total = pl->chunks * pl->V;
+    pl->nx = nx;
+    pl->ny = ny;
+    pl->nz = nz;
+    pl->nxp = round_up(nx, 32);
+    pl->cells = cells;
+    pl->cells_p = pl->nxp * ny * nz;
+    pl->steps = (int64_t)steps;
+    pl->n_recv = (int64_t)n_recv;
+    pl->nf = (int64_t)nf;
+    pl->want_ir = want_ir != 0;
+    pl->dt = grid->dt;
+    auto bail = [&](int code) {
+        delete pl;
+        return code;
+    };
+    const uint8_t *flags = grid->flags;
+    const uint32_t *bidx = grid->bidx;
+    const int64_t nb = grid->n_boundary;
+    const int64_t nslots = nb > 0 ? (int64_t)grid->bstart[nb] : 0;
+    pl->n_slots = nslots;
+
+    // Taps: merged per cell in FP64 per source (gpu_fdtd.rs:67-75), then one
+    // row per distinct cell across all sources.
+    std::unordered_map<int64_t, int64_t> tap_row;
+    std::vector<int64_t> tap_cells;
+    std::vector<double> tapw;  // [rows][lanes_total]
+    for (size_t s = 0; s < n_sources; s++) {
+        const wavey_source &src = sources[s];
+        if (src.n_taps > 0 && !src.taps) return bail(ctx->fail(WAVEY_E_INVALID, "source %zu: taps are null", s));
+        for (size_t t = 0; t < src.n_taps; t++) {
+            const int64_t c = src.taps[t].cell;
+            if (c < 0 || c >= cells) return bail(ctx->fail(WAVEY_E_INVALID, "source %zu: tap cell %lld out of range", s, (long long)c));
+            if (!(flags[c] & AIR))
+                return bail(ctx->fail(WAVEY_E_INVALID, "source %zu: tap cell %lld is not air", s, (long long)c));
+            auto it = tap_row.find(c);
+            int64_t row;
+            if (it == tap_row.end()) {
+                row = (int64_t)tap_cells.size();
+                tap_row.emplace(c, row);
+                tap_cells.push_back(c);
+                tapw.resize(tapw.size() + pl->lanes_total, 0.0);
+            } else {
+                row = it->second;
+            }
+            tapw[row * pl->lanes_total + s] += src.taps[t].w;
+        }
+    }
+    if (tap_cells.size() >= (size_t)NO_BOUNDARY) return bail(ctx->fail(WAVEY_E_LIMIT, "too many taps"));
+    for (size_t r = 0; r < n_recv; r++)
+        if (receivers[r] >= (uint64_t)cells)
+            return bail(ctx->fail(WAVEY_E_INVALID, "receiver %zu: cell %llu out of range", r, (unsigned long long)receivers[r]));
+
+    // Border cells must be solid: the reference pads every grid with one
+    // solid layer (fdtd.rs:292-299), and the kernels rely on it to keep every
+    // neighbour in range.  Boundary indices must point into the slot table.
+    std::vector<uint32_t> mask((size_t)(pl->cells_p / 32), 0u);
+    const int64_t nxw = pl->nxp / 32;
+    struct Special {
+        uint32_t cell, meta, slot0;
+    };
+    std::vector<std::vector<Special>> sp(nz);
+    std::vector<int64_t> air_z(nz, 0), int_z(nz, 0);
+    std::vector<int> bad_z(nz, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t z = 0; z < nz; z++) {
+        for (int64_t y = 0; y < ny; y++) {
+            for (int64_t x = 0; x < nx; x++) {
+                const int64_t i = (z * ny + y) * nx + x;
+                const uint8_t f = flags[i];
+                if (!(f & AIR)) continue;
+                if (x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1) {
+                    bad_z[z] = 1;
+                    continue;
+                }
+                const uint32_t b = bidx[i];
+                if (b != NO_BOUNDARY && (int64_t)b >= nb) {
+                    bad_z[z] = 2;
+                    continue;
+                }
+                air_z[z]++;
+                const int64_t ip = (z * ny + y) * pl->nxp + x;
+                if (f == (AIR | 63) && b == NO_BOUNDARY) {
+                    mask[(size_t)((z * ny + y) * nxw + x / 32)] |= 1u << (x % 32);
+                    int_z[z]++;
+                } else {
+                    const uint32_t ns = b == NO_BOUNDARY ? 0 : grid->bstart[b + 1] - grid->bstart[b];
+                    sp[z].push_back({(uint32_t)ip, (uint32_t)(f & 63) | (ns << wk::META_SLOT_SHIFT),
+                                     b == NO_BOUNDARY ? 0u : grid->bstart[b]});
+                }
+            }
+        }
+    }
+    for (int64_t z = 0; z < nz; z++) {
+        if (bad_z[z] == 1)
+            return bail(ctx->fail(WAVEY_E_INVALID,
+                                  "air cell on the grid border (plane z=%lld): the grid needs a solid padding layer",
+                                  (long long)z));
+        if (bad_z[z] == 2) return bail(ctx->fail(WAVEY_E_INVALID, "boundary index out of range in plane z=%lld", (long long)z));
+    }
+    if (pl->cells_p >= (int64_t)NO_BOUNDARY) return bail(ctx->fail(WAVEY_E_LIMIT, "padded grid exceeds 2^32 cells"));
+    // Tap cells leave the interior mask and join the special list, which
+    // stays sorted by cell.
+    std::vector<uint32_t> tap_p(tap_cells.size());
+    for (size_t r = 0; r < tap_cells.size(); r++) {
+        const int64_t c = tap_cells[r];
+        const int64_t x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);
+        tap_p[r] = (uint32_t)((z * ny + y) * pl->nxp + x);
+        uint32_t &w = mask[(size_t)((z * ny + y) * nxw + x / 32)];
+        if (w & (1u << (x % 32))) {
+            w &= ~(1u << (x % 32));
+            int_z[z]--;
+            sp[z].push_back({tap_p[r], 63u, 0u});
+            std::sort(sp[z].begin(), sp[z].end(), [](const Special &a, const Special &b) { return a.cell < b.cell; });
+        }
+    }
+    std::vector<uint32_t> cell_l, meta_l, slot0_l, tap_l;
+    for (int64_t z = 0; z < nz; z++) {
+        for (const Special &q : sp[z]) {
+            cell_l.push_back(q.cell);
+            meta_l.push_back(q.meta);
+            slot0_l.push_back(q.slot0);
+        }
+        std::vector<Special>().swap(sp[z]);
+    }
+    tap_l.assign(cell_l.size(), wk::NO_TAP);
+    for (size_t r = 0; r < tap_p.size(); r++) {
+        auto it = std::lower_bound(cell_l.begin(), cell_l.end(), tap_p[r]);
+        tap_l[(size_t)(it - cell_l.begin())] = (uint32_t)r;
+    }
+    for (int64_t z = 0; z < nz; z++) {
+        pl->air += air_z[z];
+        pl->interior += int_z[z];
+    }
+    pl->n_special = (int64_t)cell_l.size();
+    if ((int64_t)pl->n_special * pl->chunks >= (1ll << 40)) return bail(ctx->fail(WAVEY_E_LIMIT, "too many special cells"));
+
+    // Launch geometry.
+    pl->tiles_x = (int)(pl->nxp / 32);
+    pl->tiles_y = (int)((ny - 2 + wk::TILE_Y - 1) / wk::TILE_Y);
+    pl->tiles_z = (int)((nz - 2 + ZT - 1) / ZT);
+    const int64_t ib = (int64_t)pl->tiles_x * pl->tiles_y * pl->tiles_z * pl->chunks;
+    const int64_t sb = (pl->n_special * pl->chunks + wk::BLOCK - 1) / wk::BLOCK;
+    const int64_t rb = (pl->n_recv * pl->chunks + wk::BLOCK - 1) / wk::BLOCK;
+    if (ib + sb + rb >= (1ll << 31)) return bail(ctx->fail(WAVEY_E_LIMIT, "launch grid too large"));
+    pl->interior_blocks = (int)ib;
+    pl->special_blocks = (int)sb;
+    pl->record_blocks = (int)rb;
+
+    // Device buffers.
+    const size_t E = pl->elem;
+    pl->field_bytes = (size_t)pl->cells_p * pl->V * pl->chunks * E;
+    for (int k = 0; k < 2; k++)
+        if ((st = alloc(pl, &pl->field[k], pl->field_bytes))) return bail(st);
+    if ((st = upload(pl, &pl->mask, mask.data(), mask.size() * 4))) return bail(st);
+    if ((st = upload(pl, &pl->sp_cell, cell_l.data(), cell_l.size() * 4))) return bail(st);
+    if ((st = upload(pl, &pl->sp_meta, meta_l.data(), meta_l.size() * 4))) return bail(st);
+    if ((st = upload(pl, &pl->sp_slot0, slot0_l.data(), slot0_l.size() * 4))) return bail(st);
+    if ((st = upload(pl, &pl->sp_tap, tap_l.data(), tap_l.size() * 4))) return bail(st);
+    std::vector<double> slot_v(grid->slots ? grid->slots : (const double *)nullptr,
+                               grid->slots ? grid->slots + 4 * nslots : (const double *)nullptr);
+    std::vector<double> sig_v;
+    if (signal_stride == 0) {
+        sig_v.assign(signals, signals + steps);
+        pl->sig_stride = 0;
+    } else {
+        sig_v.resize((size_t)pl->lanes_total * steps, 0.0);
+        for (size_t s = 0; s < n_sources; s++)
+            std::copy(signals + s * signal_stride, signals + s * signal_stride + steps, sig_v.begin() + s * steps);
+        pl->sig_stride = (int64_t)steps;
+    }
+    std::vector<uint32_t> recv_p(n_recv);
+    for (size_t r = 0; r < n_recv; r++) {
+        const int64_t c = (int64_t)receivers[r];
+        const int64_t x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);
+        recv_p[r] = (uint32_t)((z * ny + y) * pl->nxp + x);
+    }
+    if (precision == WAVEY_FP64) {
+        if ((st = upload_typed<double>(pl, &pl->slots, slot_v))) return bail(st);
+        if ((st = upload_typed<double>(pl, &pl->tapw, tapw))) return bail(st);
+        if ((st = upload_typed<double>(pl, &pl->sig, sig_v))) return bail(st);
+    } else {
+        if ((st = upload_typed<float>(pl, &pl->slots, slot_v))) return bail(st);
+        if ((st = upload_typed<float>(pl, &pl->tapw, tapw))) return bail(st);
+        if ((st = upload_typed<float>(pl, &pl->sig, sig_v))) return bail(st);
+    }
+    if ((st = upload(pl, &pl->recv, recv_p.data(), recv_p.size() * 4))) return bail(st);
+    if ((st = upload(pl, &pl->freqs, freqs, nf * sizeof(double)))) return bail(st);
+    pl->state_bytes = (size_t)pl->chunks * nslots * pl->V * E;
+    if ((st = alloc(pl, &pl->su, pl->state_bytes))) return bail(st);
+    if ((st = alloc(pl, &pl->sg, pl->state_bytes))) return bail(st);
+    if ((st = alloc(pl, &pl->ring, (size_t)pl->chunks * wk::RING * n_recv * pl->V * E))) return bail(st);
+    if ((st = alloc(pl, &pl->tw, (size_t)wk::RING * nf * 2 * E))) return bail(st);
+    pl->acc_bytes = (size_t)pl->chunks * n_recv * nf * pl->V * 2 * sizeof(double);
+    if ((st = alloc(pl, &pl->acc, pl->acc_bytes))) return bail(st);
+    if ((st = alloc(pl, &pl->base, sizeof(long long)))) return bail(st);
+    if (pl->want_ir) {
+        pl->ir_bytes = (size_t)n_sources * n_recv * steps * E;
+        if ((st = alloc(pl, &pl->ir, pl->ir_bytes))) return bail(st);
+    }
+    for (cudaEvent_t *e : {&pl->ev_a, &pl->ev_b, &pl->ev_t0, &pl->ev_t1, &pl->inflight[0], &pl->inflight[1], &pl->inflight[2],
+                           &pl->inflight[3]})
+        if ((st = ctx->cuda(cudaEventCreate(e), "event create"))) return bail(st);
+    if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
+    if (steps >= (size_t)wk::RING)
+        if ((st = build_graph(pl))) return bail(st);
+    *out = pl;
+    return WAVEY_OK;
+}
+
+int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progress)(double, void *), void *user,
+             wavey_run_stats *stats) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    cudaStream_t s = ctx->stream;
+    int st;
+    cudaEventRecord(pl->ev_t0, s);
+    for (int k = 0; k < 2; k++)
+        if ((st = ctx->cuda(cudaMemsetAsync(pl->field[k], 0, pl->field_bytes, s), "memset"))) return st;
+    if (pl->state_bytes) {
+        if ((st = ctx->cuda(cudaMemsetAsync(pl->su, 0, pl->state_bytes, s), "memset"))) return st;
+        if ((st = ctx->cuda(cudaMemsetAsync(pl->sg, 0, pl->state_bytes, s), "memset"))) return st;
+    }
+    if ((st = ctx->cuda(cudaMemsetAsync(pl->acc, 0, pl->acc_bytes, s), "memset"))) return st;
+    if ((st = ctx->cuda(cudaMemsetAsync(pl->base, 0, sizeof(long long), s), "memset"))) return st;
+    const bool watch = cancel || progress || stats;
+    const int64_t full = pl->steps / wk::RING;
+    const int rem = (int)(pl->steps % wk::RING);
+    double step_ms = 0.0;
+    int64_t launches = 0;
+    for (int64_t c = 0; c < full; c++) {
+        if (cancel && *cancel) {
+            cudaStreamSynchronize(s);
+            return WAVEY_CANCELLED;
+        }
+        if ((st = ctx->cuda(cudaGraphLaunch(pl->graph, s), "graph launch"))) return st;
+        launches += wk::RING;
+        if (stats) {
+            if ((st = ctx->cuda(cudaEventSynchronize(pl->ev_b), "chunk wait"))) return st;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, pl->ev_a, pl->ev_b);
+            step_ms += ms;
+        } else if (watch) {
+            // At most two chunks in flight, so cancel and progress keep up.
+            cudaEventRecord(pl->inflight[c & 3], s);
+            if (c >= 1 && (st = ctx->cuda(cudaEventSynchronize(pl->inflight[(c - 1) & 3]), "chunk wait"))) return st;
+        }
+        if (progress) progress((double)((c + 1) * wk::RING) / (double)pl->steps, user);
+    }
+    if (rem > 0) {
+        if (cancel && *cancel) {
+            cudaStreamSynchronize(s);
+            return WAVEY_CANCELLED;
+        }
+        cudaEventRecord(pl->ev_a, s);
+        for (int t = 0; t < rem; t++) step(pl, t, t & 1);
+        cudaEventRecord(pl->ev_b, s);
+        fold(pl, rem);
+        launches += rem;
+        if ((st = ctx->cuda(cudaGetLastError(), "step launch"))) return st;
+        if (stats) {
+            if ((st = ctx->cuda(cudaEventSynchronize(pl->ev_b), "chunk wait"))) return st;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, pl->ev_a, pl->ev_b);
+            step_ms += ms;
+        }
+    }
+    cudaEventRecord(pl->ev_t1, s);
+    if ((st = ctx->cuda(cudaStreamSynchronize(s), "run"))) return st;
+    if ((st = ctx->cuda(cudaGetLastError(), "run"))) return st;
+    if (progress) progress(1.0, user);
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pl->ev_t0, pl->ev_t1);
+        stats->total_ms = ms;
+        stats->step_ms = step_ms;
+        stats->step_launches = launches;
+        stats->chunks = full + (rem > 0);
+    }
+    pl->ran = true;
+    return WAVEY_OK;
+}
+
+int plan_read(wavey_cuda_plan *pl, double *out, double *ir_out) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    if (!pl->ran) return ctx->fail(WAVEY_E_INVALID, "the plan has not run");
+    int st;
+    if (out && pl->acc_bytes) {
+        std::vector<double> acc(pl->acc_bytes / sizeof(double));
+        if ((st = ctx->cuda(cudaMemcpy(acc.data(), pl->acc, pl->acc_bytes, cudaMemcpyDeviceToHost), "read spectra"))) return st;
+        const int64_t R = pl->n_recv, F = pl->nf, V = pl->V;
+        for (int s = 0; s < pl->n_sources; s++) {
+            const int64_t c = s / V, l = s % V;
+            for (int64_t r = 0; r < R; r++)
+                for (int64_t f = 0; f < F; f++) {
+                    const double *a = acc.data() + ((((c * R) + r) * F + f) * V + l) * 2;
+                    double *o = out + (((int64_t)s * R + r) * F + f) * 2;
+                    o[0] = a[0];
+                    o[1] = a[1];
+                }
+        }
+    }
+    if (ir_out) {
+        if (!pl->want_ir) return ctx->fail(WAVEY_E_INVALID, "the plan records no time series");
+        const size_t n = pl->ir_bytes / pl->elem;
+        if (pl->precision == WAVEY_FP64) {
+            if ((st = ctx->cuda(cudaMemcpy(ir_out, pl->ir, pl->ir_bytes, cudaMemcpyDeviceToHost), "read ir"))) return st;
+        } else {
+            std::vector<float> v(n);
+            if ((st = ctx->cuda(cudaMemcpy(v.data(), pl->ir, pl->ir_bytes, cudaMemcpyDeviceToHost), "read ir"))) return st;
+            for (size_t i = 0; i < n; i++) ir_out[i] = (double)v[i];
+        }
+    }
+    return WAVEY_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wavey_cuda_create(int device, wavey_cuda_ctx **out) {
+    if (!out) return WAVEY_E_INVALID;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return WAVEY_E_CUDA;
+    }
+    if (device < 0 || device >= n) return WAVEY_E_INVALID;
+    wavey_cuda_ctx *ctx = new (std::nothrow) wavey_cuda_ctx();
+    if (!ctx) return WAVEY_E_NOMEM;
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete ctx;
+        return WAVEY_E_CUDA;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) {
+        ctx->sm_count = prop.multiProcessorCount;
+        snprintf(ctx->name, sizeof ctx->name, "%s", prop.name);
+    }
+    *out = ctx;
+    return WAVEY_OK;
+}
+
+void wavey_cuda_destroy(wavey_cuda_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char *wavey_cuda_last_error(const wavey_cuda_ctx *ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int wavey_cuda_device_info(wavey_cuda_ctx *ctx, char *name, size_t name_cap, int *sm_count) {
+    if (!ctx) return WAVEY_E_INVALID;
+    if (name && name_cap) snprintf(name, name_cap, "%s", ctx->name);
+    if (sm_count) *sm_count = ctx->sm_count;
+    return WAVEY_OK;
+}
+
+int wavey_cuda_plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source *sources, size_t n_sources,
+                           const double *signals, size_t signal_stride, size_t steps, const uint64_t *receivers,
+                           size_t n_recv, const double *freqs, size_t nf, int32_t precision, int32_t want_ir,
+                           wavey_cuda_plan **out) {
+    if (!ctx) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return plan_create(ctx, grid, sources, n_sources, signals, signal_stride, steps, receivers, n_recv, freqs, nf, precision,
+                       want_ir, out);
+}
+
+int wavey_cuda_plan_run(wavey_cuda_plan *plan, const volatile int32_t *cancel, void (*progress)(double, void *), void *user,
+                        wavey_run_stats *stats) {
+    if (!plan) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(plan->ctx->mu);
+    cudaSetDevice(plan->ctx->device);
+    return plan_run(plan, cancel, progress, user, stats);
+}
+
+int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out) {
+    if (!plan) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(plan->ctx->mu);
+    cudaSetDevice(plan->ctx->device);
+    return plan_read(plan, out, ir_out);
+}
+
+int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
+    if (!pl || !info) return WAVEY_E_INVALID;
+    info->cells = pl->cells;
+    info->air_cells = pl->air;
+    info->interior_cells = pl->interior;
+    info->special_cells = pl->n_special;
+    info->boundary_slots = pl->n_slots;
+    info->sources = pl->n_sources;
+    info->lanes = pl->V;
+    info->chunks = pl->chunks;
+    info->receivers = pl->n_recv;
+    info->freqs = pl->nf;
+    info->steps = pl->steps;
+    info->device_bytes = pl->device_bytes;
+    info->padded_nx = pl->nxp;
+    info->precision = pl->precision;
+    info->h2d_bytes = pl->h2d_bytes;
+    info->d2h_bytes = (int64_t)pl->acc_bytes + (int64_t)pl->ir_bytes;
+    info->graph_kernels = pl->graph_kernels;
+    return WAVEY_OK;
+}
+
+void wavey_cuda_plan_destroy(wavey_cuda_plan *plan) {
+    if (!plan) return;
+    wavey_cuda_ctx *ctx = plan->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete plan;
+}
+
+int wavey_cuda_fdtd_run_batch(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source *sources, size_t n_sources,
+                              const double *signals, size_t signal_stride, size_t steps, const uint64_t *receivers,
+                              size_t n_recv, const double *freqs, size_t nf, int32_t precision, double *out, double *ir_out,
+                              const volatile int32_t *cancel, void (*progress)(double, void *), void *user) {
+    if (!ctx) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    if (!out && n_recv * nf > 0) return ctx->fail(WAVEY_E_INVALID, "out is null");
+    wavey_cuda_plan *pl = nullptr;
+    int st = plan_create(ctx, grid, sources, n_sources, signals, signal_stride, steps, receivers, n_recv, freqs, nf,
+                         precision, ir_out != nullptr, &pl);
+    if (st) return st;
+    st = plan_run(pl, cancel, progress, user, nullptr);
+    if (st == WAVEY_OK) st = plan_read(pl, out, ir_out);
+    cudaStreamSynchronize(ctx->stream);
+    delete pl;
+    return st;
+}
+
+int wavey_cuda_fdtd_run(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_tap *taps, size_t n_taps,
+                        const double *signal, size_t steps, const uint64_t *receivers, size_t n_recv, const double *freqs,
+                        size_t nf, double *out, double *ir_out, const volatile int32_t *cancel,
+                        void (*progress)(double, void *), void *user) {
+    wavey_source src{taps, n_taps};
+    return wavey_cuda_fdtd_run_batch(ctx, grid, &src, 1, signal, 0, steps, receivers, n_recv, freqs, nf, WAVEY_FP32, out,
+                                     ir_out, cancel, progress, user);
+}
+
+}  // extern "C"

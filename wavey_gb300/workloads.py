@@ -1,0 +1,183 @@
+"""Seeded synthetic scenes with the shapes of the wave solver's benchmark
+configurations (no measured rooms or speaker data are needed).
+
+  room_small      6 x 4 x 3 m shoebox at 250 Hz, frequency-independent walls
+                  (alpha ~ U(0.05, 0.4) per surface), one monopole, 8 receivers,
+                  0.5 s                                   (~26 k air cells)
+  room_pillars    20 x 15 x 8 m with four 0.6 x 0.6 m pillars at 500 Hz, five
+                  materials with octave-band alpha ~ U(0.02, 0.6) at
+                  63..1000 Hz fitted to the boundary filter form, one cardioid
+                  (monopole + 3 dipoles = 4 right-hand sides), 64 receivers
+                  plus a 1.2 m cut plane at 0.25 m spacing, 1.0 s (~7 M cells)
+  room_hall       40 x 25 x 15 m with 12 pillars and a stepped balcony at
+                  1 kHz (~370 M cells), 8 materials
+
+Grid spacing follows the reference's points-per-wavelength rule at ppw 10
+(dx = c / (10 f_c)), the form its FDTD tests and `bras_wave` use
+(FdtdGrid::build, fdtd.rs:276-286).  Receivers are mapped to nodes with
+nearest_air (wavey-solver/src/run.rs:464); frequencies are the 1/12-octave
+grid with a non-zero crossover weight (run.rs:463).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .fdtd import (BoxRoom, FdtdGrid, FdtdSettings, component_weights, fit_first_order, frequency_grid,
+                   source_components, source_signal, speaker_rotation)
+from .materials import Material, Spectrum, fit_surfaces
+
+C_AIR = 343.0
+OCTAVES = [63.0, 125.0, 250.0, 500.0, 1000.0]
+
+
+def cardioid(_f, d):
+    """D = 0.5 + 0.5 d.x in the speaker frame (tests/fdtd.rs:485)."""
+    return complex(0.5 + 0.5 * d[0], 0.0)
+
+
+@dataclass
+class Scene:
+    name: str
+    room: BoxRoom
+    grid: FdtdGrid
+    fits: list
+    sources: list          # right-hand sides: lists of (cell, weight) taps
+    signal: np.ndarray
+    receivers: list
+    freqs: np.ndarray
+    crossover: float
+    weights: list = field(default_factory=list)   # per frequency, per component complex weight
+    notes: dict = field(default_factory=dict)
+
+    @property
+    def steps(self) -> int:
+        return len(self.signal)
+
+
+def _pillars(rng, n, room_x, room_y, size=0.6, gap=1.0, margin=1.0):
+    out = []
+    while len(out) < n:
+        x = rng.uniform(margin, room_x - margin - size)
+        y = rng.uniform(margin, room_y - margin - size)
+        if all(abs(x - p[0]) > size + gap or abs(y - p[1]) > size + gap for p in out):
+            out.append((x, y, x + size, y + size))
+    return out
+
+
+def _random_points(rng, room, n, margin=0.5):
+    pts = []
+    while len(pts) < n:
+        p = (rng.uniform(room.x0 + margin, room.x1 - margin), rng.uniform(room.y0 + margin, room.y1 - margin),
+             rng.uniform(margin, room.height - margin))
+        if room.contains(p):
+            pts.append(p)
+    return pts
+
+
+def plane_points(room, z, spacing):
+    """Inside points of a horizontal cut plane (receivers.rs:108-140)."""
+    nu = max(1, math.ceil((room.x1 - room.x0) / spacing))
+    nv = max(1, math.ceil((room.y1 - room.y0) / spacing))
+    u0 = (room.x0 + room.x1) / 2.0 - (nu - 1.0) / 2.0 * spacing
+    v0 = (room.y0 + room.y1) / 2.0 - (nv - 1.0) / 2.0 * spacing
+    pts = []
+    for iv in range(nv):
+        for iu in range(nu):
+            p = (u0 + iu * spacing, v0 + iv * spacing, z)
+            if room.contains(p):
+                pts.append(p)
+    return pts
+
+
+def wave_freqs(crossover):
+    s = FdtdSettings(crossover_hz=crossover)
+    return np.array([f for f in frequency_grid(20.0, 20000.0, 12) if s.weight(f) > 0.0])
+
+
+def _materials(rng, n):
+    return [Material(id=f"m{i}", absorption=Spectrum.bands(OCTAVES, rng.uniform(0.02, 0.6, len(OCTAVES))))
+            for i in range(n)]
+
+
+def room_small(seed: int = 1) -> Scene:
+    rng = np.random.default_rng(seed)
+    fc = 250.0
+    room = BoxRoom(6.0, 4.0, 3.0)
+    mats = [Material(id=f"a{i}", absorption=Spectrum(float(rng.uniform(0.05, 0.4)))) for i in range(6)]
+    fits = fit_surfaces(mats, (20.0, fc * math.sqrt(2.0)))
+    g = FdtdGrid.build(room, fits, C_AIR, fc, 10.0)
+    src = _random_points(rng, room, 1, margin=2 * g.dx + 0.3)[0]
+    taps = g.taps_at(src)
+    rx = [g.nearest_air(p) for p in _random_points(rng, room, 8)]
+    steps = math.ceil(0.5 / g.dt)
+    return Scene("room_small", room, g, fits, [taps], source_signal(fc, g.dt, steps), rx, wave_freqs(fc), fc,
+                 notes={"seed": seed, "source": src})
+
+
+def room_pillars(seed: int = 2, duration: float = 1.0, n_materials: int = 5, plane_spacing: float = 0.25,
+                 n_mics: int = 64) -> Scene:
+    rng = np.random.default_rng(seed)
+    fc = 500.0
+    pillars = _pillars(rng, 4, 20.0, 15.0)
+    room = BoxRoom(20.0, 15.0, 8.0, pillars=pillars)
+    mats = _materials(rng, n_materials)
+    assign = [mats[int(k)] for k in rng.integers(0, n_materials, room.n_surfaces)]
+    fits = fit_surfaces(assign, (20.0, fc * math.sqrt(2.0)))
+    g = FdtdGrid.build(room, fits, C_AIR, fc, 10.0)
+    pos = _random_points(rng, room, 1, margin=2.0)[0]
+    yaw, pitch = float(rng.uniform(0, 360)), float(rng.uniform(-30, 30))
+    node = g.nearest_air(pos)
+    comps = source_components(g, node, 1)
+    if comps is None:
+        raise RuntimeError("source too close to a surface for a directional source")
+    mics = [g.nearest_air(p) for p in _random_points(rng, room, n_mics)]
+    plane = [g.nearest_air(p) for p in plane_points(room, 1.2, plane_spacing)]
+    freqs = wave_freqs(fc)
+    steps = math.ceil(duration / g.dt)
+    rot = speaker_rotation(yaw, pitch, 0.0)
+    weights = []
+    for f in freqs:
+        a0, a, _res = fit_first_order(cardioid, rot, f)
+        weights.append(component_weights(a0, a, 2.0 * math.pi * f / C_AIR, g.dx))
+    return Scene("room_pillars", room, g, fits, comps, source_signal(fc, g.dt, steps), mics + plane, freqs, fc,
+                 weights=weights,
+                 notes={"seed": seed, "pillars": pillars, "source": pos, "yaw": yaw, "pitch": pitch,
+                        "mics": len(mics), "plane_points": len(plane)})
+
+
+def room_pillars_speakers(n_speakers: int, seed: int = 4, duration: float = 1.0) -> Scene:
+    """room_pillars' room and materials with n seeded speakers; each speaker
+    is a monopole or a cardioid (4 right-hand sides)."""
+    base = room_pillars(seed=2, duration=duration)
+    rng = np.random.default_rng(seed)
+    g = base.grid
+    sources = []
+    kinds = []
+    for _ in range(n_speakers):
+        pos = _random_points(rng, base.room, 1, margin=1.5)[0]
+        node = g.nearest_air(pos)
+        if rng.uniform() < 0.5:
+            sources.append(g.taps_at(pos))
+            kinds.append("monopole")
+        else:
+            sources.extend(source_components(g, node, 1))
+            kinds.append("cardioid")
+    base.name = f"room_pillars_{n_speakers}spk"
+    base.sources = sources
+    base.weights = []
+    base.notes = dict(base.notes, speakers=kinds)
+    return base
+
+
+def octave_levels(transfer: np.ndarray, freqs: np.ndarray, centres) -> np.ndarray:
+    """10 log10 of the mean |H|^2 over the bins of each octave band
+    (band_edges(f, 1), freq.rs:32-35); transfer [..., nf]."""
+    out = []
+    for fc in centres:
+        lo, hi = fc / 2 ** 0.5, fc * 2 ** 0.5
+        sel = (freqs >= lo) & (freqs < hi)
+        out.append(10.0 * np.log10(np.mean(np.abs(transfer[..., sel]) ** 2, axis=-1)))
+    return np.stack(out, axis=-1)
