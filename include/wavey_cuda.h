@@ -126,6 +126,29 @@ int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out);
 int wavey_cuda_plan_info(const wavey_cuda_plan *plan, wavey_plan_info *info);
 void wavey_cuda_plan_destroy(wavey_cuda_plan *plan);
 
+/* Receiver spectra from receiver time series, allocating no device memory.
+ * No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory when they need the spectra, such as a real-time
+ * audio thread (cudaMalloc/cudaFree can stall the device) or a host whose
+ * own pool allocator owns all device memory.
+ *
+ * series (device, [n_recv][steps] FP32) holds p^n per receiver, freqs
+ * (device, [nf]) the bins, out (device, [n_recv][nf][2] FP64) receives
+ * sum_n p^n exp(-j 2 pi frac(f dt n)), the running DFT of fdtd.rs:673-683,
+ * computed as the FDTD runs compute it (FP32 sums over 128-step chunks added
+ * into FP64).  stream may be NULL (the default stream).  At most
+ * WAVEY_NOALLOC_MAX_FREQS frequencies (WAVEY_E_LIMIT beyond).  err (nullable)
+ * receives a message on failure.
+ *
+ * Scratch is one fixed 2 MiB array inside the library (every GPU that loads
+ * the library holds it until exit).  The first call on a device looks up
+ * that array's device address, so make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
+#define WAVEY_NOALLOC_MAX_FREQS 2048
+int wavey_cuda_receiver_dft_noalloc(int device, const float *series, int64_t n_recv, int64_t steps, const double *freqs,
+                                    int64_t nf, double dt, double *out, void *stream, char *err, size_t err_cap);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,7 +37,7 @@ def _cuda_cmd(out: Path) -> list[str]:
         nvcc(), *ARCH, "-lineinfo", "-O3", "-std=c++17", "-shared",
         "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off,-O2",
         "-I", str(INCLUDE),
-        str(CSRC / "wavey_cuda.cu"), "-o", str(out), "-lgomp",
+        str(CSRC / "wavey_cuda.cu"), str(CSRC / "receiver_dft_noalloc.cu"), "-o", str(out), "-lgomp",
     ]
 
 
@@ -70,7 +70,7 @@ def build(force: bool = False, cuda: bool = True) -> dict[str, Path]:
         jobs[host_out] = _host_cmd(host_out)
     cuda_out = LIB / "libwavey_cuda.so"
     if cuda:
-        cuda_deps = [CSRC / "wavey_cuda.cu", CSRC / "fdtd_kernels.cuh"] + list(INCLUDE.glob("*.h"))
+        cuda_deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
         if force or _stale(cuda_out, cuda_deps):
             jobs[cuda_out] = _cuda_cmd(cuda_out)
     if jobs:

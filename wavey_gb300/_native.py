@@ -193,6 +193,8 @@ def cuda() -> C.CDLL:
         "wavey_cuda_plan_read": (C.c_int, [vp, c_double_p, c_double_p]),
         "wavey_cuda_plan_info": (C.c_int, [vp, C.POINTER(WaveyPlanInfo)]),
         "wavey_cuda_plan_destroy": (None, [vp]),
+        "wavey_cuda_receiver_dft_noalloc": (C.c_int, [C.c_int, C.POINTER(C.c_float), C.c_int64, C.c_int64, c_double_p,
+                                                      C.c_int64, C.c_double, c_double_p, vp, C.c_char_p, C.c_size_t]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
