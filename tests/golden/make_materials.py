@@ -1,7 +1,7 @@
-"""Writes tests/golden/materials.json: the octave-band absorption tables of
-the reference's built-in materials that its FDTD tests use
-(core/wavey-materials/src/library.json, read through
-core/wavey-materials/src/library.rs:7-13).
+"""Writes tests/golden/materials.json: the absorption tables of the
+reference's built-in materials (core/wavey-materials/src/library.json, read
+through core/wavey-materials/src/library.rs:7-13), which its FDTD tests and
+its impedance-fit unit tests (impedance_fit.rs:242-283) use.
 
 Run here, where the reference is mounted; the JSON is committed so the
 tests never read the reference at run time.
@@ -11,12 +11,9 @@ import sys
 from pathlib import Path
 
 REF = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference") / "core/wavey-materials/src/library.json"
-USED = ["audience-standing", "mineral-wool-50", "mineral-wool-100", "carpet-heavy", "curtain-heavy",
-        "gypsum-board", "wood-panel", "plaster-rough", "ceiling-industrial"]
-
 lib = {m["id"]: m for m in json.loads(REF.read_text())}
 out = {}
-for mid in USED:
+for mid in lib:
     a = lib[mid]["absorption"]
     out[mid] = a if isinstance(a, (int, float)) else {"freqs_hz": a["freqs_hz"], "values": a["values"]}
 Path(__file__).with_name("materials.json").write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
