@@ -15,8 +15,10 @@ right-hand sides, batched in one launch per time step, FP32.  The fields
             kernels run on), in G/s
   e2e       the same metric through the C-ABI call wavey_cuda_fdtd_run_batch
             with host buffers: packing, upload, run and read-back inside
-  roofline  the fused step kernel: 12 B per air-cell update per source
-            (read p, read and write the older buffer) / its mean launch time
+  roofline  one time step (the TMA-fed interior kernel and, beside it, the
+            special-cell/receiver kernel): 12 B per air-cell update per
+            source (read p, read and write the older buffer) / the mean step
+            span measured with CUDA events around each chunk's step launches
   plain     the same four right-hand sides run one at a time (S = 1 kernel)
 
 --impl reference times the reference's CPU algorithm (the oracle's C
@@ -335,8 +337,9 @@ def run_ours(args, rank, world):
             "hbm_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "fdtd_step<float,4>", "bytes_per_launch": alg_bytes,
-                         "mean_launch_us": launch_s * 1e6},
+                         "kernel": ("step = interior_tma || fdtd_step special/record branch" if info["interior_kernel"]
+                                    else "fdtd_step<float,4> (fused)"),
+                         "bytes_per_launch": alg_bytes, "mean_launch_us": launch_s * 1e6},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": info["h2d_bytes"],
                     "d2h_bytes_per_step": info["d2h_bytes"], "seconds": e2e_s},
             "accuracy": acc,

@@ -86,6 +86,9 @@ typedef struct {
     int64_t h2d_bytes;                    /* host-to-device bytes of plan_create */
     int64_t d2h_bytes;                    /* device-to-host bytes of plan_read */
     int64_t graph_kernels;                /* kernels per replay of the 128-step graph */
+    int32_t interior_kernel;              /* 1: TMA-fed z-march beside the special-cell kernel; 0: fused step kernel */
+    int32_t tma_zt;                       /* z planes per CTA of the TMA kernel */
+    int32_t tma_depth;                    /* ring depth of the TMA kernel (0: 6/4, 1: 8/6, 2: 11/9 planes) */
 } wavey_plan_info;
 
 int wavey_cuda_create(int device, wavey_cuda_ctx **out);

@@ -104,6 +104,7 @@ class WaveyPlanInfo(C.Structure):
         ("receivers", C.c_int64), ("freqs", C.c_int64), ("steps", C.c_int64),
         ("device_bytes", C.c_int64), ("padded_nx", C.c_int64), ("precision", C.c_int32),
         ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("graph_kernels", C.c_int64),
+        ("interior_kernel", C.c_int32), ("tma_zt", C.c_int32), ("tma_depth", C.c_int32),
     ]
 
 

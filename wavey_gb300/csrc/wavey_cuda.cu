@@ -29,6 +29,7 @@
 
 #include "../../include/wavey_cuda.h"
 #include "fdtd_kernels.cuh"
+#include "interior_tma.cuh"
 
 namespace {
 
@@ -38,10 +39,39 @@ constexpr uint32_t NO_BOUNDARY = 0xFFFFFFFFu;
 constexpr uint8_t AIR = 64;
 constexpr int ZT = 16;  // z planes marched by one interior CTA
 
-struct Status {
-    int code;
-    std::string msg;
-};
+// cuTensorMapEncodeTiled, fetched from the driver once (no link-time
+// dependency on libcuda).
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled() {
+    static EncodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// Interior kernel variant of FP32 runs: the TMA-fed z-march (default) or the
+// register-queue z-march inside the fused step kernel.
+bool tma_selected() {
+    const char *v = getenv("WAVEY_INTERIOR");
+    return !(v && strcmp(v, "regq") == 0);
+}
+
+int env_int(const char *name, int dflt, int lo, int hi) {
+    const char *v = getenv(name);
+    if (!v) return dflt;
+    int x = atoi(v);
+    return x < lo ? lo : (x > hi ? hi : x);
+}
 
 }  // namespace
 
@@ -49,6 +79,7 @@ struct wavey_cuda_ctx {
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;  // the special-cell branch of a TMA step
     std::mutex mu;
     std::string err;
     char name[256] = {0};
@@ -100,6 +131,14 @@ struct wavey_cuda_plan {
     int interior_blocks = 0, special_blocks = 0, record_blocks = 0;
     cudaGraphExec_t graph = nullptr;
     int64_t graph_kernels = 0;  // kernel launches per replay of the chunk graph
+    // TMA interior path (FP32)
+    bool tma = false;
+    CUtensorMap tm_p[2], tm_q[2];  // per parity: p^n of field[parity], old of field[parity^1]
+    int tma_tiles_x = 0, tma_tiles_y = 0, tma_tiles_z = 0, tma_zt = 32, tma_blocks = 0;
+    int tma_cfg = 0;      // shape of the TMA kernel, an index into TMA_CFGS
+    int special_prio = 0;       // launch priority of the special-cell branch
+    int *err = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
     cudaEvent_t inflight[4] = {nullptr, nullptr, nullptr, nullptr};
     bool ran = false;
@@ -108,7 +147,7 @@ struct wavey_cuda_plan {
 
     ~wavey_cuda_plan() {
         if (graph) cudaGraphExecDestroy(graph);
-        for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1, inflight[0], inflight[1], inflight[2], inflight[3]})
+        for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1, inflight[0], inflight[1], inflight[2], inflight[3], ev_fork, ev_join})
             if (e) cudaEventDestroy(e);
         for (DevBuf &b : bufs)
             if (b.p) cudaFree(b.p);
@@ -214,7 +253,100 @@ void launch_step(wavey_cuda_plan *pl, int t, int parity) {
     if (blocks > 0) wk::fdtd_step<T, V, RUST><<<blocks, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
 }
 
+// Shapes of the TMA interior kernel: rows per tile and ring depths.
+struct TmaCfg {
+    int rows, np, nq;
+};
+constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4}, {8, 8, 4}, {16, 6, 4}, {16, 8, 4}, {16, 5, 3}};
+constexpr int TMA_NCFG = 5;
+
+template <int V, int R, int NP, int NQ>
+void launch_tma(int blocks, cudaStream_t s, const CUtensorMap &p, const CUtensorMap &q, const wk::TmaArgs &ta) {
+    wk::interior_tma<V, R, NP, NQ><<<blocks, 256, wk::tma_smem_of<R, NP, NQ>(), s>>>(p, q, ta);
+}
+
+template <int V>
+void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, const CUtensorMap &p, const CUtensorMap &q, const wk::TmaArgs &ta) {
+    switch (cfg) {
+        case 1: launch_tma<V, 8, 8, 4>(blocks, s, p, q, ta); break;
+        case 2: launch_tma<V, 16, 6, 4>(blocks, s, p, q, ta); break;
+        case 3: launch_tma<V, 16, 8, 4>(blocks, s, p, q, ta); break;
+        case 4: launch_tma<V, 16, 5, 3>(blocks, s, p, q, ta); break;
+        default: launch_tma<V, 8, 6, 4>(blocks, s, p, q, ta); break;
+    }
+}
+
+template <int V, int R, int NP, int NQ>
+cudaError_t tma_attr() {
+    return cudaFuncSetAttribute((const void *)wk::interior_tma<V, R, NP, NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)wk::tma_smem_of<R, NP, NQ>());
+}
+
+template <int V>
+cudaError_t tma_attrs() {
+    cudaError_t e[] = {tma_attr<V, 8, 6, 4>(), tma_attr<V, 8, 8, 4>(), tma_attr<V, 16, 6, 4>(), tma_attr<V, 16, 8, 4>(),
+                       tma_attr<V, 16, 5, 3>()};
+    for (cudaError_t x : e)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
+}
+
+template <int V>
+void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
+    cudaStream_t s = pl->ctx->stream, side = pl->ctx->side;
+    const bool branch = pl->special_blocks + pl->record_blocks > 0;
+    if (branch) {
+        // Special cells and receiver samples on a concurrent branch (the fused
+        // kernel's special and record roles): they read only p^n and write
+        // cells the interior kernel does not touch.
+        cudaEventRecord(pl->ev_fork, s);
+        cudaStreamWaitEvent(side, pl->ev_fork, 0);
+        wk::StepArgs<float> a;
+        fill_args<float>(pl, a, parity);
+        a.interior_blocks = 0;
+        cudaLaunchConfig_t lc = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributePriority;
+        attr[0].val.priority = pl->special_prio;
+        lc.blockDim = dim3(wk::BLOCK);
+        lc.stream = side;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        lc.gridDim = dim3(pl->special_blocks + pl->record_blocks);
+        cudaLaunchKernelEx(&lc, wk::fdtd_step<float, V, false>, a, t);
+    }
+    if (pl->tma_blocks > 0) {
+        wk::TmaArgs ta;
+        ta.interior = pl->mask;
+        ta.nxt = reinterpret_cast<float *>(pl->field[parity ^ 1]);
+        ta.error = pl->err;
+        ta.cells_p = pl->cells_p;
+        ta.nxp = (int)pl->nxp;
+        ta.ny = (int)pl->ny;
+        ta.nz = (int)pl->nz;
+        ta.nxw = (int)(pl->nxp / 32);
+        ta.tiles_x = pl->tma_tiles_x;
+        ta.tiles_y = pl->tma_tiles_y;
+        ta.tiles_z = pl->tma_tiles_z;
+        ta.zt = pl->tma_zt;
+        ta.l2 = (float)(COURANT * COURANT);
+        launch_tma_cfg<V>(pl->tma_cfg, pl->tma_blocks, s, pl->tm_p[parity], pl->tm_q[parity], ta);
+    }
+    if (branch) {
+        cudaEventRecord(pl->ev_join, side);
+        cudaStreamWaitEvent(s, pl->ev_join, 0);
+    }
+}
+
 void step(wavey_cuda_plan *pl, int t, int parity) {
+    if (pl->tma) {
+        switch (pl->V) {
+            case 1: launch_step_tma<1>(pl, t, parity); break;
+            case 2: launch_step_tma<2>(pl, t, parity); break;
+            default: launch_step_tma<4>(pl, t, parity); break;
+        }
+        return;
+    }
     if (pl->precision == WAVEY_FP64) {
         switch (pl->V) {
             case 1: launch_step<double, 1, true>(pl, t, parity); break;
@@ -282,7 +414,15 @@ int build_graph(wavey_cuda_plan *pl) {
     if (e != cudaSuccess) return ctx->cuda(e, "end capture");
     size_t nodes = 0;
     cudaGraphGetNodes(g, nullptr, &nodes);
-    pl->graph_kernels = (int64_t)nodes - 2;  // minus the two event-record nodes
+    pl->graph_kernels = 0;
+    {
+        std::vector<cudaGraphNode_t> list(nodes);
+        cudaGraphGetNodes(g, list.data(), &nodes);
+        for (cudaGraphNode_t n : list) {
+            cudaGraphNodeType ty;
+            if (cudaGraphNodeGetType(n, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) pl->graph_kernels++;
+        }
+    }
     e = cudaGraphInstantiate(&pl->graph, g, 0);
     cudaGraphDestroy(g);
     return ctx->cuda(e, "graph instantiate");
@@ -536,6 +676,48 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     for (cudaEvent_t *e : {&pl->ev_a, &pl->ev_b, &pl->ev_t0, &pl->ev_t1, &pl->inflight[0], &pl->inflight[1], &pl->inflight[2],
                            &pl->inflight[3]})
         if ((st = ctx->cuda(cudaEventCreate(e), "event create"))) return bail(st);
+    for (cudaEvent_t *e : {&pl->ev_fork, &pl->ev_join})
+        if ((st = ctx->cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event create"))) return bail(st);
+    if ((st = alloc(pl, &pl->err, sizeof(int)))) return bail(st);
+    if (precision == WAVEY_FP32 && tma_selected()) {
+        EncodeTiled enc = encode_tiled();
+        if (!enc) return bail(ctx->fail(WAVEY_E_CUDA, "the driver lacks cuTensorMapEncodeTiled"));
+        const int V = pl->V;
+        const cuuint64_t dims[4] = {(cuuint64_t)(nx * V), (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)pl->chunks};
+        const cuuint64_t strides[3] = {(cuuint64_t)(pl->nxp * V * 4), (cuuint64_t)(pl->nxp * ny * V * 4),
+                                       (cuuint64_t)(pl->cells_p * V * 4)};
+        pl->tma_cfg = env_int("WAVEY_TMA_CFG", 0, 0, TMA_NCFG - 1);
+        const int rows = TMA_CFGS[pl->tma_cfg].rows;
+        const cuuint32_t box_p[4] = {(cuuint32_t)wk::TMA_P_ROW, (cuuint32_t)(rows + 2), 1, 1};
+        const cuuint32_t box_q[4] = {(cuuint32_t)wk::TMA_ROW_FLOATS, (cuuint32_t)rows, 1, 1};
+        const cuuint32_t unit[4] = {1, 1, 1, 1};
+        for (int k = 0; k < 2; k++) {
+            CUresult r1 = enc(&pl->tm_p[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k], dims, strides, box_p, unit,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            CUresult r2 = enc(&pl->tm_q[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k ^ 1], dims, strides, box_q, unit,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS)
+                return bail(ctx->fail(WAVEY_E_CUDA, "tensor map encoding failed (%d, %d)", (int)r1, (int)r2));
+        }
+        pl->tma_zt = env_int("WAVEY_TMA_ZT", 16, 1, 4096);
+        pl->tma_tiles_x = (int)((nx + (wk::TMA_ROW_FLOATS / V) - 1) / (wk::TMA_ROW_FLOATS / V));
+        pl->tma_tiles_y = (int)((ny - 2 + rows - 1) / rows);
+        pl->tma_tiles_z = (int)((nz - 2 + pl->tma_zt - 1) / pl->tma_zt);
+        const int64_t tb = (int64_t)pl->tma_tiles_x * pl->tma_tiles_y * pl->tma_tiles_z * pl->chunks;
+        if (tb >= (1ll << 31)) return bail(ctx->fail(WAVEY_E_LIMIT, "launch grid too large"));
+        pl->tma_blocks = (int)tb;
+
+        cudaError_t e = tma_attrs<1>();
+        if (e == cudaSuccess) e = tma_attrs<2>();
+        if (e == cudaSuccess) e = tma_attrs<4>();
+        int lo_prio = 0, hi_prio = 0;
+        cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+        pl->special_prio = env_int("WAVEY_SPECIAL_PRIO", 0, 0, 1) ? hi_prio : lo_prio;
+        if ((st = ctx->cuda(e, "shared memory attribute"))) return bail(st);
+        pl->tma = true;
+    }
     if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
     if (steps >= (size_t)wk::RING)
         if ((st = build_graph(pl))) return bail(st);
@@ -557,6 +739,7 @@ int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progres
     }
     if ((st = ctx->cuda(cudaMemsetAsync(pl->acc, 0, pl->acc_bytes, s), "memset"))) return st;
     if ((st = ctx->cuda(cudaMemsetAsync(pl->base, 0, sizeof(long long), s), "memset"))) return st;
+    if ((st = ctx->cuda(cudaMemsetAsync(pl->err, 0, sizeof(int), s), "memset"))) return st;
     const bool watch = cancel || progress || stats;
     const int64_t full = pl->steps / wk::RING;
     const int rem = (int)(pl->steps % wk::RING);
@@ -602,6 +785,9 @@ int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progres
     cudaEventRecord(pl->ev_t1, s);
     if ((st = ctx->cuda(cudaStreamSynchronize(s), "run"))) return st;
     if ((st = ctx->cuda(cudaGetLastError(), "run"))) return st;
+    int err_word = 0;
+    if ((st = ctx->cuda(cudaMemcpy(&err_word, pl->err, sizeof(int), cudaMemcpyDeviceToHost), "error word"))) return st;
+    if (err_word) return ctx->fail(WAVEY_E_DEVICE, "a kernel reported error %d (a bounded wait ran out)", err_word);
     if (progress) progress(1.0, user);
     if (stats) {
         float ms = 0.f;
@@ -664,7 +850,8 @@ int wavey_cuda_create(int device, wavey_cuda_ctx **out) {
     wavey_cuda_ctx *ctx = new (std::nothrow) wavey_cuda_ctx();
     if (!ctx) return WAVEY_E_NOMEM;
     ctx->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return WAVEY_E_CUDA;
@@ -682,6 +869,7 @@ void wavey_cuda_destroy(wavey_cuda_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     delete ctx;
 }
 
@@ -739,6 +927,9 @@ int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
     info->h2d_bytes = pl->h2d_bytes;
     info->d2h_bytes = (int64_t)pl->acc_bytes + (int64_t)pl->ir_bytes;
     info->graph_kernels = pl->graph_kernels;
+    info->interior_kernel = pl->tma ? 1 : 0;
+    info->tma_zt = pl->tma ? pl->tma_zt : 0;
+    info->tma_depth = pl->tma ? pl->tma_cfg : -1;
     return WAVEY_OK;
 }
 
