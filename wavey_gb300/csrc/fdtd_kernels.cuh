@@ -154,6 +154,102 @@ __device__ __forceinline__ Lanes<T, V> interior_update(const Lanes<T, V> &c, con
     return o;
 }
 
+// One special cell k of chunk c at step n (the special role of fdtd_step).
+template <class T, int V, bool RUST_ORDER>
+__device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, long long n) {
+    const long long nxy = (long long)a.nxp * a.ny;
+    const int c = (int)(k / a.n_special);
+    k -= (long long)c * a.n_special;
+    const long long cell = a.sp_cell[k];
+    const uint32_t m = a.sp_meta[k];
+    const T *P = a.cur + (long long)c * a.cells_p * V;
+    T *Q = a.nxt + (long long)c * a.cells_p * V;
+    const Lanes<T, V> pc = load<T, V, true>(P + cell * V);
+    const Lanes<T, V> pp = load<T, V, false>(Q + cell * V);
+    const long long offs[6] = {-1, 1, -(long long)a.nxp, (long long)a.nxp, -nxy, nxy};
+    Lanes<T, V> sum;
+#pragma unroll
+    for (int l = 0; l < V; l++) sum.v[l] = T(0);
+    T kk = T(0);
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+        if ((m >> d) & 1u) {
+            Lanes<T, V> nb = load<T, V, true>(P + (cell + offs[d]) * V);
+#pragma unroll
+            for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb.v[l]);
+            kk = radd(kk, T(1));
+        }
+    }
+    Lanes<T, V> lap, next;
+#pragma unroll
+    for (int l = 0; l < V; l++) lap.v[l] = rmul(a.l2, rsub(sum.v[l], rmul(kk, pc.v[l])));
+    const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
+    const T half = T(0.5), two = T(2), one = T(1);
+    if (ns == 0) {
+#pragma unroll
+        for (int l = 0; l < V; l++) next.v[l] = radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]);
+    } else {
+        const long long j0 = a.sp_slot0[k];
+        T *SU = a.su + (long long)c * a.n_slots * V;
+        T *SG = a.sg + (long long)c * a.n_slots * V;
+        T s1 = T(0);
+        Lanes<T, V> s2;
+#pragma unroll
+        for (int l = 0; l < V; l++) s2.v[l] = T(0);
+        for (int q = 0; q < ns; q++) {
+            const long long j = j0 + q;
+            const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
+            const Lanes<T, V> u = load<T, V, false>(SU + j * V);
+            const Lanes<T, V> g = load<T, V, false>(SG + j * V);
+#pragma unroll
+            for (int l = 0; l < V; l++) {
+                T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
+                s2.v[l] = RUST_ORDER ? radd(s2.v[l], rsub(e, u.v[l])) : rsub(radd(s2.v[l], e), u.v[l]);
+            }
+            s1 = radd(s1, rmul(rsub(half, w), inv_d));
+        }
+        const T den = radd(one, rmul(a.lam, s1));
+#pragma unroll
+        for (int l = 0; l < V; l++)
+            next.v[l] = rdiv(rsub(radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]), rmul(a.lam, s2.v[l])), den);
+        for (int q = 0; q < ns; q++) {
+            const long long j = j0 + q;
+            const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
+            Lanes<T, V> u = load<T, V, false>(SU + j * V);
+            Lanes<T, V> g = load<T, V, false>(SG + j * V);
+#pragma unroll
+            for (int l = 0; l < V; l++) {
+                T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
+                T un = radd(rmul(rmul(rsub(half, w), inv_d), next.v[l]), e);
+                g.v[l] = radd(g.v[l], rmul(a.half_dt, radd(un, u.v[l])));
+                u.v[l] = un;
+            }
+            store<T, V>(SU + j * V, u);
+            store<T, V>(SG + j * V, g);
+        }
+    }
+    const uint32_t tap = a.sp_tap[k];
+    if (tap != NO_TAP) {
+#pragma unroll
+        for (int l = 0; l < V; l++) {
+            const int s = c * V + l;
+            const T sv = a.sig[(long long)s * a.sig_stride + n];
+            next.v[l] = radd(next.v[l], rmul(sv, a.tapw[(long long)tap * a.lanes_total + s]));
+        }
+    }
+    store<T, V>(Q + cell * V, next);
+}
+
+// One receiver r of chunk c into ring slot t (the record role of fdtd_step).
+template <class T, int V>
+__device__ __forceinline__ void record_one(const StepArgs<T> &a, long long k, int t) {
+    const int c = (int)(k / a.n_recv);
+    const long long r = k - (long long)c * a.n_recv;
+    const T *P = a.cur + (long long)c * a.cells_p * V;
+    const Lanes<T, V> v = load<T, V, true>(P + (long long)a.recv[r] * V);
+    store<T, V>(a.ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
+}
+
 // ------------------------------------------------------------------ step
 // RUST_ORDER selects the CPU reference's association of the branch sum
 // (s2 + (e - u), fdtd.rs:588) instead of the shader's ((s2 + e) - u,
@@ -213,99 +309,16 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step(StepArgs<T> a, int t) {
     const long long n = *a.base + t;
     if (b < a.special_blocks) {
         // ----------------------------------------------------- special
-        long long k = (long long)b * BLOCK + threadIdx.x;
+        const long long k = (long long)b * BLOCK + threadIdx.x;
         if (k >= (long long)a.n_special * a.chunks) return;
-        const int c = (int)(k / a.n_special);
-        k -= (long long)c * a.n_special;
-        const long long cell = a.sp_cell[k];
-        const uint32_t m = a.sp_meta[k];
-        const T *P = a.cur + (long long)c * a.cells_p * V;
-        T *Q = a.nxt + (long long)c * a.cells_p * V;
-        const Lanes<T, V> pc = load<T, V, true>(P + cell * V);
-        const Lanes<T, V> pp = load<T, V, false>(Q + cell * V);
-        const long long offs[6] = {-1, 1, -(long long)a.nxp, (long long)a.nxp, -nxy, nxy};
-        Lanes<T, V> sum;
-#pragma unroll
-        for (int l = 0; l < V; l++) sum.v[l] = T(0);
-        T kk = T(0);
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
-            if ((m >> d) & 1u) {
-                Lanes<T, V> nb = load<T, V, true>(P + (cell + offs[d]) * V);
-#pragma unroll
-                for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb.v[l]);
-                kk = radd(kk, T(1));
-            }
-        }
-        Lanes<T, V> lap, next;
-#pragma unroll
-        for (int l = 0; l < V; l++) lap.v[l] = rmul(a.l2, rsub(sum.v[l], rmul(kk, pc.v[l])));
-        const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
-        const T half = T(0.5), two = T(2), one = T(1);
-        if (ns == 0) {
-#pragma unroll
-            for (int l = 0; l < V; l++) next.v[l] = radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]);
-        } else {
-            const long long j0 = a.sp_slot0[k];
-            T *SU = a.su + (long long)c * a.n_slots * V;
-            T *SG = a.sg + (long long)c * a.n_slots * V;
-            T s1 = T(0);
-            Lanes<T, V> s2;
-#pragma unroll
-            for (int l = 0; l < V; l++) s2.v[l] = T(0);
-            for (int q = 0; q < ns; q++) {
-                const long long j = j0 + q;
-                const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
-                const Lanes<T, V> u = load<T, V, false>(SU + j * V);
-                const Lanes<T, V> g = load<T, V, false>(SG + j * V);
-#pragma unroll
-                for (int l = 0; l < V; l++) {
-                    T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
-                    s2.v[l] = RUST_ORDER ? radd(s2.v[l], rsub(e, u.v[l])) : rsub(radd(s2.v[l], e), u.v[l]);
-                }
-                s1 = radd(s1, rmul(rsub(half, w), inv_d));
-            }
-            const T den = radd(one, rmul(a.lam, s1));
-#pragma unroll
-            for (int l = 0; l < V; l++)
-                next.v[l] = rdiv(rsub(radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]), rmul(a.lam, s2.v[l])), den);
-            for (int q = 0; q < ns; q++) {
-                const long long j = j0 + q;
-                const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
-                Lanes<T, V> u = load<T, V, false>(SU + j * V);
-                Lanes<T, V> g = load<T, V, false>(SG + j * V);
-#pragma unroll
-                for (int l = 0; l < V; l++) {
-                    T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
-                    T un = radd(rmul(rmul(rsub(half, w), inv_d), next.v[l]), e);
-                    g.v[l] = radd(g.v[l], rmul(a.half_dt, radd(un, u.v[l])));
-                    u.v[l] = un;
-                }
-                store<T, V>(SU + j * V, u);
-                store<T, V>(SG + j * V, g);
-            }
-        }
-        const uint32_t tap = a.sp_tap[k];
-        if (tap != NO_TAP) {
-#pragma unroll
-            for (int l = 0; l < V; l++) {
-                const int s = c * V + l;
-                const T sv = a.sig[(long long)s * a.sig_stride + n];
-                next.v[l] = radd(next.v[l], rmul(sv, a.tapw[(long long)tap * a.lanes_total + s]));
-            }
-        }
-        store<T, V>(Q + cell * V, next);
+        special_cell<T, V, RUST_ORDER>(a, k, *a.base + t);
         return;
     }
     b -= a.special_blocks;
     // --------------------------------------------------------- record
-    long long k = (long long)b * BLOCK + threadIdx.x;
+    const long long k = (long long)b * BLOCK + threadIdx.x;
     if (k >= (long long)a.n_recv * a.chunks) return;
-    const int c = (int)(k / a.n_recv);
-    const long long r = k - (long long)c * a.n_recv;
-    const T *P = a.cur + (long long)c * a.cells_p * V;
-    const Lanes<T, V> v = load<T, V, true>(P + (long long)a.recv[r] * V);
-    store<T, V>(a.ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
+    record_one<T, V>(a, k, t);
 }
 
 // ------------------------------------------------------------- twiddles
