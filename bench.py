@@ -310,6 +310,31 @@ def run_ours(args, rank, world):
                "spectra_worst_rel": float(np.abs(spec32 - spec64).max() / np.abs(spec64).max()),
                "reference": "FP64 GPU run of the same grid (WAVEY_FP64)"}
 
+    # FP16 field storage: throughput and its error against the FP64 run.
+    fp16 = None
+    if not args.no_fp16:
+        from wavey_gb300.backend import FP16_STORAGE
+
+        p16 = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP16_STORAGE)
+        p16.run()
+        st16 = p16.run(stats=True)
+        spec16 = p16.read()
+        p16.close()
+        fp16 = {"value": updates_per_run / (st16["total_ms"] / 1e3) / 1e9, "unit": UNIT,
+                "bytes_per_update": 6, "kernel": "fdtd_step_half (fused, register-queue z-march)"}
+        if acc is not None:
+            h0 = np.ones(len(scene.freqs), complex)
+            t16 = np.stack([to_transfer(spec16[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
+            t64b = np.stack([to_transfer(spec64[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
+            if scene.weights:
+                t16 = np.einsum("fs,srf->rf", np.array(scene.weights), t16)
+                t64b = np.einsum("fs,srf->rf", np.array(scene.weights), t64b)
+            cent = [c for c in W.OCTAVES if c <= scene.crossover]
+            d = np.abs(W.octave_levels(t16, scene.freqs, cent) - W.octave_levels(t64b, scene.freqs, cent))
+            fp16["octave_band_max_abs_db"] = float(d.max())
+            fp16["octave_band_p99_abs_db"] = float(np.quantile(d, 0.99))
+            fp16["spectra_worst_rel"] = float(np.abs(spec16 - spec64).max() / np.abs(spec64).max())
+
     # CPU baseline (rank 0 at N = 1): the oracle on a bounded sample.
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -343,6 +368,7 @@ def run_ours(args, rank, world):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": info["h2d_bytes"],
                     "d2h_bytes_per_step": info["d2h_bytes"], "seconds": e2e_s},
             "accuracy": acc,
+            "fp16_storage": fp16,
             "cpu_baseline": cpu,
             "gpu_launches": int(kernels_per_run * args.steps),
             "clocks": clocks.summary(),
@@ -364,6 +390,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp16", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 (timing rule)")

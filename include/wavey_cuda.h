@@ -66,6 +66,8 @@ typedef struct {
 /* Storage precision of the fields. */
 #define WAVEY_FP32 0          /* FP32 throughout, the reference GPU's arithmetic order */
 #define WAVEY_FP64 1          /* FP64 throughout, the reference CPU's order: the GPU oracle */
+#define WAVEY_FP16_STORAGE 2  /* fields stored in FP16 with a power-of-two scale per z slab; FP32 updates,
+                                 FP32 branch states, FP64 spectra */
 
 /* Per-run timing, filled when a stats pointer is given (the run then waits
  * for each 128-step chunk to read its events). */

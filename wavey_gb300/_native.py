@@ -27,6 +27,7 @@ WAVEY_E_DEVICE = -5
 
 WAVEY_FP32 = 0
 WAVEY_FP64 = 1
+WAVEY_FP16_STORAGE = 2
 
 WH_MAX_BRANCHES = 4
 WH_FIT_DIRECTIONS = 400

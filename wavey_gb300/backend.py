@@ -23,6 +23,7 @@ from . import _native as N
 
 FP32 = N.WAVEY_FP32
 FP64 = N.WAVEY_FP64
+FP16_STORAGE = N.WAVEY_FP16_STORAGE
 
 
 class WaveyError(RuntimeError):

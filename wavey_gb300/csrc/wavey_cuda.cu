@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "../../include/wavey_cuda.h"
+#include "fdtd_half.cuh"
 #include "fdtd_kernels.cuh"
 #include "interior_tma.cuh"
 
@@ -125,7 +126,12 @@ struct wavey_cuda_plan {
     double *acc = nullptr, *freqs = nullptr;
     long long *base = nullptr;
     int64_t sig_stride = 0;
-    size_t field_bytes = 0, state_bytes = 0, acc_bytes = 0, ir_bytes = 0, elem = 4;
+    size_t field_bytes = 0, state_bytes = 0, acc_bytes = 0, ir_bytes = 0;
+    size_t elem = 4;        // bytes of the arithmetic type (slots, states, ring, spectra inputs)
+    size_t field_elem = 4;  // bytes of a stored field value (2 in FP16 storage)
+    unsigned int *amax = nullptr;  // FP16 storage: slab maxima ring
+    float2 *scale = nullptr;       // FP16 storage: slab scale ring
+    float *wmax = nullptr;         // FP16 storage: sum |tap weight| per source
     // launch geometry
     int tiles_x = 0, tiles_y = 0, tiles_z = 0;
     int interior_blocks = 0, special_blocks = 0, record_blocks = 0;
@@ -338,12 +344,69 @@ void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
     }
 }
 
+template <int V>
+void launch_step_half(wavey_cuda_plan *pl, int t, int parity) {
+    wk::HalfArgs a;
+    a.cur = reinterpret_cast<const __half *>(pl->field[parity]);
+    a.nxt = reinterpret_cast<__half *>(pl->field[parity ^ 1]);
+    a.interior = pl->mask;
+    a.sp_cell = pl->sp_cell;
+    a.sp_meta = pl->sp_meta;
+    a.sp_slot0 = pl->sp_slot0;
+    a.sp_tap = pl->sp_tap;
+    a.slots = reinterpret_cast<const float *>(pl->slots);
+    a.su = reinterpret_cast<float *>(pl->su);
+    a.sg = reinterpret_cast<float *>(pl->sg);
+    a.tapw = reinterpret_cast<const float *>(pl->tapw);
+    a.sig = reinterpret_cast<const float *>(pl->sig);
+    a.wmax = pl->wmax;
+    a.recv = pl->recv;
+    a.ring = reinterpret_cast<float *>(pl->ring);
+    a.base = pl->base;
+    a.amax = pl->amax;
+    a.scale = pl->scale;
+    a.error = pl->err;
+    a.cells_p = pl->cells_p;
+    a.sig_stride = pl->sig_stride;
+    a.nxp = (int)pl->nxp;
+    a.ny = (int)pl->ny;
+    a.nz = (int)pl->nz;
+    a.nxw = (int)(pl->nxp / 32);
+    a.n_special = (int)pl->n_special;
+    a.n_slots = (int)pl->n_slots;
+    a.n_recv = (int)pl->n_recv;
+    a.chunks = pl->chunks;
+    a.lanes_total = pl->lanes_total;
+    a.tiles_x = pl->tiles_x;
+    a.tiles_y = pl->tiles_y;
+    a.tiles_z = pl->tiles_z;
+    a.zt = ZT;
+    a.interior_blocks = pl->interior_blocks;
+    a.special_blocks = pl->special_blocks;
+    a.record_blocks = pl->record_blocks;
+    a.l2 = (float)(COURANT * COURANT);
+    a.lam = (float)COURANT;
+    a.half_dt = 0.5f * (float)pl->dt;
+    const int prep = (int)((pl->chunks * pl->nz + wk::BLOCK - 1) / wk::BLOCK);
+    wk::half_prepare<V><<<prep, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
+    const int blocks = pl->interior_blocks + pl->special_blocks + pl->record_blocks;
+    if (blocks > 0) wk::fdtd_step_half<V><<<blocks, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
+}
+
 void step(wavey_cuda_plan *pl, int t, int parity) {
     if (pl->tma) {
         switch (pl->V) {
             case 1: launch_step_tma<1>(pl, t, parity); break;
             case 2: launch_step_tma<2>(pl, t, parity); break;
             default: launch_step_tma<4>(pl, t, parity); break;
+        }
+        return;
+    }
+    if (pl->precision == WAVEY_FP16_STORAGE) {
+        switch (pl->V) {
+            case 1: launch_step_half<1>(pl, t, parity); break;
+            case 2: launch_step_half<2>(pl, t, parity); break;
+            default: launch_step_half<4>(pl, t, parity); break;
         }
         return;
     }
@@ -384,7 +447,7 @@ void launch_fold(wavey_cuda_plan *pl, int count) {
 }
 
 void fold(wavey_cuda_plan *pl, int count) {
-    if (pl->precision == WAVEY_FP64) {
+    if (pl->precision == WAVEY_FP64) {  // FP32 and FP16 storage fold in FP32
         switch (pl->V) {
             case 1: launch_fold<double, 1>(pl, count); break;
             case 2: launch_fold<double, 2>(pl, count); break;
@@ -453,7 +516,8 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     *out = nullptr;
     int st = validate_grid(ctx, grid);
     if (st) return st;
-    if (precision != WAVEY_FP32 && precision != WAVEY_FP64) return ctx->fail(WAVEY_E_INVALID, "unknown precision %d", precision);
+    if (precision != WAVEY_FP32 && precision != WAVEY_FP64 && precision != WAVEY_FP16_STORAGE)
+        return ctx->fail(WAVEY_E_INVALID, "unknown precision %d", precision);
     if (n_sources == 0 || !sources) return ctx->fail(WAVEY_E_INVALID, "no sources");
     if (n_sources > 4096) return ctx->fail(WAVEY_E_LIMIT, "at most 4096 sources per run");
     if (steps > 0 && !signals) return ctx->fail(WAVEY_E_INVALID, "signals are null");
@@ -470,6 +534,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     pl->ctx = ctx;
     pl->precision = precision;
     pl->elem = precision == WAVEY_FP64 ? 8 : 4;
+    pl->field_elem = precision == WAVEY_FP64 ? 8 : (precision == WAVEY_FP16_STORAGE ? 2 : 4);
     pl->n_sources = (int)n_sources;
     pl->V = n_sources >= 4 ? 4 : (n_sources == 1 ? 1 : (n_sources == 2 ? 2 : 4));
     pl->chunks = (int)((n_sources + pl->V - 1) / pl->V);
@@ -624,7 +689,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
 
     // Device buffers.
     const size_t E = pl->elem;
-    pl->field_bytes = (size_t)pl->cells_p * pl->V * pl->chunks * E;
+    pl->field_bytes = (size_t)pl->cells_p * pl->V * pl->chunks * pl->field_elem;
     for (int k = 0; k < 2; k++)
         if ((st = alloc(pl, &pl->field[k], pl->field_bytes))) return bail(st);
     if ((st = upload(pl, &pl->mask, mask.data(), mask.size() * 4))) return bail(st);
@@ -658,6 +723,18 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if ((st = upload_typed<float>(pl, &pl->slots, slot_v))) return bail(st);
         if ((st = upload_typed<float>(pl, &pl->tapw, tapw))) return bail(st);
         if ((st = upload_typed<float>(pl, &pl->sig, sig_v))) return bail(st);
+    }
+    if (precision == WAVEY_FP16_STORAGE) {
+        std::vector<float> wm((size_t)pl->lanes_total, 0.0f);
+        for (size_t s2 = 0; s2 < n_sources; s2++) {
+            double acc = 0.0;
+            for (size_t t2 = 0; t2 < sources[s2].n_taps; t2++) acc += std::fabs(sources[s2].taps[t2].w);
+            wm[s2] = (float)(acc * (1.0 + 1e-6));
+        }
+        if ((st = upload(pl, &pl->wmax, wm.data(), wm.size() * 4))) return bail(st);
+        if ((st = alloc(pl, &pl->amax, (size_t)wk::AMAX_RING * pl->chunks * nz * sizeof(unsigned int)))) return bail(st);
+        if ((st = alloc(pl, &pl->scale, (size_t)wk::SCALE_RING * pl->chunks * nz * sizeof(float2)))) return bail(st);
+        if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
     }
     if ((st = upload(pl, &pl->recv, recv_p.data(), recv_p.size() * 4))) return bail(st);
     if ((st = upload(pl, &pl->freqs, freqs, nf * sizeof(double)))) return bail(st);
@@ -740,6 +817,15 @@ int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progres
     if ((st = ctx->cuda(cudaMemsetAsync(pl->acc, 0, pl->acc_bytes, s), "memset"))) return st;
     if ((st = ctx->cuda(cudaMemsetAsync(pl->base, 0, sizeof(long long), s), "memset"))) return st;
     if ((st = ctx->cuda(cudaMemsetAsync(pl->err, 0, sizeof(int), s), "memset"))) return st;
+    if (pl->amax) {
+        // Levels 0 and -1 are all zeros: any scale reads them back as zeros.
+        if ((st = ctx->cuda(cudaMemsetAsync(pl->amax, 0, (size_t)wk::AMAX_RING * pl->chunks * pl->nz * sizeof(unsigned int), s),
+                            "memset")))
+            return st;
+        if ((st = ctx->cuda(cudaMemsetAsync(pl->scale, 0, (size_t)wk::SCALE_RING * pl->chunks * pl->nz * sizeof(float2), s),
+                            "memset")))
+            return st;
+    }
     const bool watch = cancel || progress || stats;
     const int64_t full = pl->steps / wk::RING;
     const int rem = (int)(pl->steps % wk::RING);
@@ -787,6 +873,8 @@ int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progres
     if ((st = ctx->cuda(cudaGetLastError(), "run"))) return st;
     int err_word = 0;
     if ((st = ctx->cuda(cudaMemcpy(&err_word, pl->err, sizeof(int), cudaMemcpyDeviceToHost), "error word"))) return st;
+    if (err_word == wk::ERR_FP16_RANGE)
+        return ctx->fail(WAVEY_E_DEVICE, "a field value left the FP16 range of its slab scale");
     if (err_word) return ctx->fail(WAVEY_E_DEVICE, "a kernel reported error %d (a bounded wait ran out)", err_word);
     if (progress) progress(1.0, user);
     if (stats) {
