@@ -131,6 +131,38 @@ int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out);
 int wavey_cuda_plan_info(const wavey_cuda_plan *plan, wavey_plan_info *info);
 void wavey_cuda_plan_destroy(wavey_cuda_plan *plan);
 
+/* Several rooms in one launch per time step: the rooms' step blocks are laid
+ * end to end in one grid (a work-tile table; each block finds its room), so
+ * rooms of uneven sizes, each with its own right-hand sides, signals,
+ * receivers and step count, fill the GPU together.  It replaces running
+ * `GridRunner` once per room (fdtd.rs:884-885; e.g. the per-cabinet
+ * calibration pairs of fdtd.rs:941-942).  FP32 or FP64. */
+typedef struct wavey_cuda_rooms wavey_cuda_rooms;
+typedef struct {
+    const wavey_grid *grid;
+    const wavey_source *sources;
+    size_t n_sources;
+    const double *signals;     /* as wavey_cuda_fdtd_run_batch */
+    size_t signal_stride;
+    size_t steps;
+    const uint64_t *receivers;
+    size_t n_recv;
+    const double *freqs;
+    size_t nf;
+    double *out;               /* [S][n_recv][nf][2], written by wavey_cuda_fdtd_run_rooms */
+    double *ir_out;            /* nullable [S][n_recv][steps] */
+} wavey_room_job;
+
+int wavey_cuda_fdtd_run_rooms(wavey_cuda_ctx *ctx, const wavey_room_job *jobs, size_t n_jobs, int32_t precision,
+                              const volatile int32_t *cancel, void (*progress)(double, void *), void *user);
+int wavey_cuda_rooms_create(wavey_cuda_ctx *ctx, const wavey_room_job *jobs, size_t n_jobs, int32_t precision,
+                            int32_t want_ir, wavey_cuda_rooms **out);
+int wavey_cuda_rooms_run(wavey_cuda_rooms *rooms, const volatile int32_t *cancel, void (*progress)(double, void *),
+                         void *user, wavey_run_stats *stats);
+int wavey_cuda_rooms_read(wavey_cuda_rooms *rooms, size_t room, double *out, double *ir_out);
+int wavey_cuda_rooms_info(const wavey_cuda_rooms *rooms, size_t room, wavey_plan_info *info);
+void wavey_cuda_rooms_destroy(wavey_cuda_rooms *rooms);
+
 /* Receiver spectra from receiver time series, allocating no device memory.
  * No counterpart in the reference: it exists for callers that cannot
  * allocate device memory when they need the spectra, such as a real-time

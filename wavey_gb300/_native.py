@@ -93,6 +93,15 @@ class WaveySource(C.Structure):
     _fields_ = [("taps", C.POINTER(WaveyTap)), ("n_taps", C.c_size_t)]
 
 
+class WaveyRoomJob(C.Structure):
+    _fields_ = [
+        ("grid", C.POINTER(WaveyGrid)), ("sources", C.POINTER(WaveySource)), ("n_sources", C.c_size_t),
+        ("signals", c_double_p), ("signal_stride", C.c_size_t), ("steps", C.c_size_t),
+        ("receivers", c_uint64_p), ("n_recv", C.c_size_t), ("freqs", c_double_p), ("nf", C.c_size_t),
+        ("out", c_double_p), ("ir_out", c_double_p),
+    ]
+
+
 class WaveyRunStats(C.Structure):
     _fields_ = [("total_ms", C.c_double), ("step_ms", C.c_double), ("step_launches", C.c_int64), ("chunks", C.c_int64)]
 
@@ -195,6 +204,14 @@ def cuda() -> C.CDLL:
         "wavey_cuda_plan_read": (C.c_int, [vp, c_double_p, c_double_p]),
         "wavey_cuda_plan_info": (C.c_int, [vp, C.POINTER(WaveyPlanInfo)]),
         "wavey_cuda_plan_destroy": (None, [vp]),
+        "wavey_cuda_fdtd_run_rooms": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, cancel_p,
+                                                PROGRESS_FN, vp]),
+        "wavey_cuda_rooms_create": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, C.c_int32,
+                                              C.POINTER(vp)]),
+        "wavey_cuda_rooms_run": (C.c_int, [vp, cancel_p, PROGRESS_FN, vp, C.POINTER(WaveyRunStats)]),
+        "wavey_cuda_rooms_read": (C.c_int, [vp, C.c_size_t, c_double_p, c_double_p]),
+        "wavey_cuda_rooms_info": (C.c_int, [vp, C.c_size_t, C.POINTER(WaveyPlanInfo)]),
+        "wavey_cuda_rooms_destroy": (None, [vp]),
         "wavey_cuda_receiver_dft_noalloc": (C.c_int, [C.c_int, C.POINTER(C.c_float), C.c_int64, C.c_int64, c_double_p,
                                                       C.c_int64, C.c_double, c_double_p, vp, C.c_char_p, C.c_size_t]),
     }

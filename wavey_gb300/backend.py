@@ -163,6 +163,112 @@ class CudaBackend:
     def plan(self, grid, sources, signal, receivers, freqs, precision=FP32, ir: bool = False) -> "Plan":
         return Plan(self, grid, sources, signal, receivers, freqs, precision, ir)
 
+    def run_rooms(self, jobs, precision=FP32, cancel=None, progress=None, ir: bool = False):
+        """Several rooms in one launch per step.  jobs: list of RoomJob.
+        Returns per room spectra [S, n_recv, nf] (and time series), or None
+        when cancelled."""
+        packed = _pack_jobs(jobs, ir)
+        cflag, cb = _callbacks(cancel, progress)
+        with self._lock:
+            st = self._check(self._lib.wavey_cuda_fdtd_run_rooms(self._h, packed.arr, len(jobs), int(precision),
+                                                                   cflag, cb, None))
+        if st == N.WAVEY_CANCELLED:
+            return None
+        return [(o, i) if ir else o for o, i in zip(packed.outs, packed.irs)]
+
+    def rooms_plan(self, jobs, precision=FP32, ir: bool = False) -> "RoomsPlan":
+        return RoomsPlan(self, jobs, precision, ir)
+
+
+class RoomJob:
+    """One room of a multi-room run: the arguments of run_batch."""
+
+    def __init__(self, grid, sources, signal, receivers, freqs):
+        self.grid, self.sources, self.signal, self.receivers, self.freqs = grid, sources, signal, receivers, freqs
+
+
+class _Packed:
+    pass
+
+
+def _pack_jobs(jobs, ir):
+    pk = _Packed()
+    pk.keep, pk.outs, pk.irs = [], [], []
+    pk.arr = (N.WaveyRoomJob * len(jobs))()
+    for r, j in enumerate(jobs):
+        g, kg = _grid_struct(j.grid)
+        srcs, ks = _sources_struct(j.sources)
+        steps = np.asarray(j.signal).shape[-1]
+        sig, stride = _signals(j.signal, len(j.sources), steps)
+        rx = np.ascontiguousarray(j.receivers, dtype=np.uint64)
+        fr = np.ascontiguousarray(j.freqs, dtype=np.float64)
+        out = np.zeros((len(j.sources), len(rx), len(fr)), dtype=np.complex128)
+        irb = np.zeros((len(j.sources), len(rx), steps)) if ir else None
+        pk.keep += [g, kg, srcs, ks, sig, rx, fr]
+        pk.outs.append(out)
+        pk.irs.append(irb)
+        a = pk.arr[r]
+        a.grid = C.pointer(g)
+        a.sources = C.cast(srcs, C.POINTER(N.WaveySource))
+        a.n_sources = len(j.sources)
+        a.signals = N.ptr(sig, C.c_double)
+        a.signal_stride = stride
+        a.steps = steps
+        a.receivers = N.ptr(rx, C.c_uint64)
+        a.n_recv = len(rx)
+        a.freqs = N.ptr(fr, C.c_double)
+        a.nf = len(fr)
+        a.out = N.ptr(out.view(np.float64), C.c_double)
+        a.ir_out = N.ptr(irb, C.c_double)
+    return pk
+
+
+class RoomsPlan:
+    """A multi-room run kept on the device (wavey_cuda_rooms_*)."""
+
+    def __init__(self, backend: CudaBackend, jobs, precision, ir):
+        self._b = backend
+        self._packed = _pack_jobs(jobs, ir)
+        self.ir = ir
+        h = C.c_void_p()
+        with backend._lock:
+            backend._check(backend._lib.wavey_cuda_rooms_create(backend._h, self._packed.arr, len(jobs), int(precision),
+                                                                int(ir), C.byref(h)))
+        self._h = h
+        self.n = len(jobs)
+
+    def run(self, cancel=None, progress=None, stats: bool = False):
+        cflag, cb = _callbacks(cancel, progress)
+        s = N.WaveyRunStats()
+        with self._b._lock:
+            st = self._b._check(self._b._lib.wavey_cuda_rooms_run(self._h, cflag, cb, None,
+                                                                  C.byref(s) if stats else None))
+        if st == N.WAVEY_CANCELLED:
+            return None
+        if stats:
+            return {"total_ms": s.total_ms, "step_ms": s.step_ms, "step_launches": s.step_launches, "chunks": s.chunks}
+        return True
+
+    def read(self, room: int):
+        out, irb = self._packed.outs[room], self._packed.irs[room]
+        with self._b._lock:
+            self._b._check(self._b._lib.wavey_cuda_rooms_read(self._h, room, N.ptr(out.view(np.float64), C.c_double),
+                                                              N.ptr(irb, C.c_double)))
+        return (out.copy(), irb.copy()) if self.ir else out.copy()
+
+    def info(self, room: int = 0) -> dict:
+        i = N.WaveyPlanInfo()
+        self._b._lib.wavey_cuda_rooms_info(self._h, room, C.byref(i))
+        return {k: getattr(i, k) for k, _ in N.WaveyPlanInfo._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._b._lib.wavey_cuda_rooms_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
 
 class Plan:
     """A run kept on the device: inputs uploaded once, run() repeatable."""

@@ -255,8 +255,7 @@ __device__ __forceinline__ void record_one(const StepArgs<T> &a, long long k, in
 // (s2 + (e - u), fdtd.rs:588) instead of the shader's ((s2 + e) - u,
 // fdtd.wgsl:94).
 template <class T, int V, bool RUST_ORDER>
-__global__ void __launch_bounds__(BLOCK) fdtd_step(StepArgs<T> a, int t) {
-    int b = blockIdx.x;
+__device__ __forceinline__ void step_block(const StepArgs<T> &a, int b, int t) {
     const long long nxy = (long long)a.nxp * a.ny;
     if (b < a.interior_blocks) {
         // ---------------------------------------------------- interior
@@ -321,11 +320,49 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step(StepArgs<T> a, int t) {
     record_one<T, V>(a, k, t);
 }
 
+template <class T, int V, bool RUST_ORDER>
+__global__ void __launch_bounds__(BLOCK) fdtd_step(StepArgs<T> a, int t) {
+    step_block<T, V, RUST_ORDER>(a, blockIdx.x, t);
+}
+
+// ----------------------------------------------------------- many rooms
+// Several rooms advance in one launch per step.  The grid is the rooms'
+// blocks laid end to end (the work-tile table: room r owns blocks
+// [first, first + blocks)); a block finds its room, then runs the same three
+// roles on that room's arguments.  Rooms keep their own lanes per chunk and
+// their own step count: past its last step a room's blocks do nothing.
+template <class T>
+struct RoomStep {
+    StepArgs<T> a[2];  // by buffer parity
+    int lanes;         // V of the room's chunks: 1, 2 or 4
+    int blocks;
+    long long steps;
+};
+
+template <class T, bool RUST_ORDER>
+__global__ void __launch_bounds__(BLOCK) fdtd_step_rooms(const RoomStep<T> *rooms, int n_rooms, int t, int parity) {
+    int b = blockIdx.x, r = 0;
+    while (r < n_rooms - 1 && b >= rooms[r].blocks) {
+        b -= rooms[r].blocks;
+        r++;
+    }
+    const RoomStep<T> &room = rooms[r];
+    if (*room.a[0].base + t >= room.steps) return;
+    const StepArgs<T> &a = room.a[parity];
+    switch (room.lanes) {
+        case 1: step_block<T, 1, RUST_ORDER>(a, b, t); break;
+        case 2: step_block<T, 2, RUST_ORDER>(a, b, t); break;
+        default: step_block<T, 4, RUST_ORDER>(a, b, t); break;
+    }
+}
+
 // ------------------------------------------------------------- twiddles
 // tw[t][f] = exp(-j 2 pi frac(f dt n)) for n = base + t, phase in FP64
 // exactly as fdtd.rs:680 forms it.
 template <class T>
-__global__ void twiddle_chunk(const double *freqs, int nf, double dt, const long long *base, int count, T *tw) {
+__global__ void twiddle_chunk(const double *freqs, int nf, double dt, const long long *base, int count, long long steps,
+                              T *tw) {
+    count = (int)min((long long)count, steps - *base);  // a room that stops inside the chunk
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= count * nf) return;
     const int t = idx / nf, f = idx - t * nf;
@@ -342,7 +379,8 @@ __global__ void twiddle_chunk(const double *freqs, int nf, double dt, const long
 // chunk in T, added into FP64.  One thread per (chunk, receiver, freq).
 template <class T, int V>
 __global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const T *tw, double *acc, int n_recv, int nf, int chunks,
-                                                   int count) {
+                                                   int count, const long long *base, long long steps) {
+    count = (int)min((long long)count, steps - *base);
     const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
     const long long total = (long long)chunks * n_recv * nf;
     if (idx >= total) return;
@@ -375,11 +413,14 @@ __global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const T *tw, d
 template <class T, int V>
 __global__ void ir_chunk(const T *ring, T *ir, int n_recv, int chunks, int n_sources, long long steps,
                          const long long *base, int count) {
+    const int full = count;
+    count = (int)min((long long)count, steps - *base);
     const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
-    const long long total = (long long)chunks * V * n_recv * count;
+    const long long total = (long long)chunks * V * n_recv * full;
     if (idx >= total) return;
-    const int t = (int)(idx % count);
-    long long rest = idx / count;
+    const int t = (int)(idx % full);
+    if (t >= count) return;
+    long long rest = idx / full;
     const int r = (int)(rest % n_recv);
     rest /= n_recv;
     const int s = (int)rest;  // c * V + l

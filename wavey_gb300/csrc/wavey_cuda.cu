@@ -160,6 +160,32 @@ struct wavey_cuda_plan {
     }
 };
 
+// Several rooms advanced together: their plans (buffers and packing), one
+// shared step counter, the device table of RoomStep entries and one graph per
+// 128-step chunk whose step launches cover every room's blocks.
+struct wavey_cuda_rooms {
+    wavey_cuda_ctx *ctx = nullptr;
+    int precision = WAVEY_FP32;
+    std::vector<wavey_cuda_plan *> plans;
+    long long *base = nullptr;
+    void *table = nullptr;
+    int total_blocks = 0;
+    int64_t max_steps = 0;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_kernels = 0;
+    cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
+    bool ran = false;
+
+    ~wavey_cuda_rooms() {
+        if (graph) cudaGraphExecDestroy(graph);
+        for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1})
+            if (e) cudaEventDestroy(e);
+        if (base) cudaFree(base);
+        if (table) cudaFree(table);
+        for (wavey_cuda_plan *p : plans) delete p;
+    }
+};
+
 namespace {
 
 template <class T>
@@ -431,12 +457,12 @@ void launch_fold(wavey_cuda_plan *pl, int count) {
     const int tw_threads = count * (int)pl->nf;
     if (tw_threads > 0)
         wk::twiddle_chunk<T><<<(tw_threads + 255) / 256, 256, 0, s>>>(pl->freqs, (int)pl->nf, pl->dt, pl->base, count,
-                                                                       reinterpret_cast<T *>(pl->tw));
+                                                                       (long long)pl->steps, reinterpret_cast<T *>(pl->tw));
     const long long total = (long long)pl->chunks * pl->n_recv * pl->nf;
     if (total > 0)
         wk::dft_chunk<T, V><<<(unsigned)((total + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
             reinterpret_cast<const T *>(pl->ring), reinterpret_cast<const T *>(pl->tw), pl->acc, (int)pl->n_recv, (int)pl->nf,
-            pl->chunks, count);
+            pl->chunks, count, pl->base, (long long)pl->steps);
     if (pl->want_ir) {
         const long long n = (long long)pl->chunks * V * pl->n_recv * count;
         if (n > 0)
@@ -509,9 +535,13 @@ int upload_typed(wavey_cuda_plan *pl, void **out, const std::vector<double> &src
     return pl->ctx->cuda(cudaStreamSynchronize(pl->ctx->stream), "upload sync");
 }
 
+// standalone: a plan that runs by itself (TMA interior path where it
+// applies, its own chunk graph).  Plans inside a rooms plan are not
+// standalone: the rooms plan launches their fused step blocks together.
 int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source *sources, size_t n_sources,
                 const double *signals, size_t signal_stride, size_t steps, const uint64_t *receivers, size_t n_recv,
-                const double *freqs, size_t nf, int32_t precision, int32_t want_ir, wavey_cuda_plan **out) {
+                const double *freqs, size_t nf, int32_t precision, int32_t want_ir, wavey_cuda_plan **out,
+                bool standalone = true) {
     if (!out) return ctx->fail(WAVEY_E_INVALID, "out is null");
     *out = nullptr;
     int st = validate_grid(ctx, grid);
@@ -756,7 +786,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     for (cudaEvent_t *e : {&pl->ev_fork, &pl->ev_join})
         if ((st = ctx->cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event create"))) return bail(st);
     if ((st = alloc(pl, &pl->err, sizeof(int)))) return bail(st);
-    if (precision == WAVEY_FP32 && tma_selected()) {
+    if (standalone && precision == WAVEY_FP32 && tma_selected()) {
         EncodeTiled enc = encode_tiled();
         if (!enc) return bail(ctx->fail(WAVEY_E_CUDA, "the driver lacks cuTensorMapEncodeTiled"));
         const int V = pl->V;
@@ -796,18 +826,18 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         pl->tma = true;
     }
     if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
-    if (steps >= (size_t)wk::RING)
+    if (standalone && steps >= (size_t)wk::RING)
         if ((st = build_graph(pl))) return bail(st);
     *out = pl;
     return WAVEY_OK;
 }
 
-int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progress)(double, void *), void *user,
-             wavey_run_stats *stats) {
+// Clears a plan's fields, branch states, spectra, step counter, error word
+// and scale tables: every run starts from rest.
+int plan_reset(wavey_cuda_plan *pl) {
     wavey_cuda_ctx *ctx = pl->ctx;
     cudaStream_t s = ctx->stream;
     int st;
-    cudaEventRecord(pl->ev_t0, s);
     for (int k = 0; k < 2; k++)
         if ((st = ctx->cuda(cudaMemsetAsync(pl->field[k], 0, pl->field_bytes, s), "memset"))) return st;
     if (pl->state_bytes) {
@@ -826,6 +856,16 @@ int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progres
                             "memset")))
             return st;
     }
+    return WAVEY_OK;
+}
+
+int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progress)(double, void *), void *user,
+             wavey_run_stats *stats) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    cudaStream_t s = ctx->stream;
+    int st;
+    cudaEventRecord(pl->ev_t0, s);
+    if ((st = plan_reset(pl))) return st;
     const bool watch = cancel || progress || stats;
     const int64_t full = pl->steps / wk::RING;
     const int rem = (int)(pl->steps % wk::RING);
@@ -919,6 +959,159 @@ int plan_read(wavey_cuda_plan *pl, double *out, double *ir_out) {
             for (size_t i = 0; i < n; i++) ir_out[i] = (double)v[i];
         }
     }
+    return WAVEY_OK;
+}
+
+
+// ----------------------------------------------------------------- rooms
+template <class T, bool RUST>
+int rooms_table(wavey_cuda_rooms *rm) {
+    std::vector<wk::RoomStep<T>> table(rm->plans.size());
+    rm->total_blocks = 0;
+    for (size_t r = 0; r < rm->plans.size(); r++) {
+        wavey_cuda_plan *pl = rm->plans[r];
+        for (int parity = 0; parity < 2; parity++) {
+            fill_args<T>(pl, table[r].a[parity], parity);
+            table[r].a[parity].base = rm->base;
+        }
+        table[r].lanes = pl->V;
+        table[r].blocks = pl->interior_blocks + pl->special_blocks + pl->record_blocks;
+        table[r].steps = pl->steps;
+        if ((int64_t)rm->total_blocks + table[r].blocks >= (1ll << 31)) return rm->ctx->fail(WAVEY_E_LIMIT, "launch grid too large");
+        rm->total_blocks += table[r].blocks;
+    }
+    const size_t bytes = table.size() * sizeof(wk::RoomStep<T>);
+    cudaError_t e = cudaMalloc(&rm->table, bytes);
+    if (e != cudaSuccess) return rm->ctx->cuda(e, "rooms table");
+    return rm->ctx->cuda(cudaMemcpy(rm->table, table.data(), bytes, cudaMemcpyHostToDevice), "rooms table");
+}
+
+void rooms_step(wavey_cuda_rooms *rm, int t) {
+    if (rm->total_blocks == 0) return;
+    cudaStream_t s = rm->ctx->stream;
+    const int n = (int)rm->plans.size();
+    if (rm->precision == WAVEY_FP64)
+        wk::fdtd_step_rooms<double, true><<<rm->total_blocks, wk::BLOCK, 0, s>>>(
+            reinterpret_cast<const wk::RoomStep<double> *>(rm->table), n, t, t & 1);
+    else
+        wk::fdtd_step_rooms<float, false><<<rm->total_blocks, wk::BLOCK, 0, s>>>(
+            reinterpret_cast<const wk::RoomStep<float> *>(rm->table), n, t, t & 1);
+}
+
+int rooms_graph(wavey_cuda_rooms *rm) {
+    wavey_cuda_ctx *ctx = rm->ctx;
+    cudaStream_t s = ctx->stream;
+    cudaGraph_t g = nullptr;
+    int st = ctx->cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    if (st) return st;
+    cudaEventRecordWithFlags(rm->ev_a, s, cudaEventRecordExternal);
+    for (int t = 0; t < wk::RING; t++) rooms_step(rm, t);
+    cudaEventRecordWithFlags(rm->ev_b, s, cudaEventRecordExternal);
+    for (wavey_cuda_plan *pl : rm->plans) fold(pl, wk::RING);  // each stops at its own last step
+    wk::advance_base<<<1, 1, 0, s>>>(rm->base, wk::RING);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (e != cudaSuccess) return ctx->cuda(e, "end capture");
+    size_t nodes = 0;
+    cudaGraphGetNodes(g, nullptr, &nodes);
+    std::vector<cudaGraphNode_t> list(nodes);
+    cudaGraphGetNodes(g, list.data(), &nodes);
+    rm->graph_kernels = 0;
+    for (cudaGraphNode_t nd : list) {
+        cudaGraphNodeType ty;
+        if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) rm->graph_kernels++;
+    }
+    e = cudaGraphInstantiate(&rm->graph, g, 0);
+    cudaGraphDestroy(g);
+    return ctx->cuda(e, "graph instantiate");
+}
+
+int rooms_create(wavey_cuda_ctx *ctx, const wavey_room_job *jobs, size_t n_jobs, int32_t precision, int32_t want_ir,
+                 wavey_cuda_rooms **out) {
+    if (!out) return ctx->fail(WAVEY_E_INVALID, "out is null");
+    *out = nullptr;
+    if (!jobs || n_jobs == 0) return ctx->fail(WAVEY_E_INVALID, "no rooms");
+    if (n_jobs > 1024) return ctx->fail(WAVEY_E_LIMIT, "at most 1024 rooms per launch");
+    if (precision != WAVEY_FP32 && precision != WAVEY_FP64)
+        return ctx->fail(WAVEY_E_INVALID, "rooms run in FP32 or FP64 (precision %d)", precision);
+    wavey_cuda_rooms *rm = new (std::nothrow) wavey_cuda_rooms();
+    if (!rm) return ctx->fail(WAVEY_E_NOMEM, "host allocation failed");
+    rm->ctx = ctx;
+    rm->precision = precision;
+    auto bail = [&](int code) {
+        delete rm;
+        return code;
+    };
+    int st;
+    for (size_t r = 0; r < n_jobs; r++) {
+        const wavey_room_job &j = jobs[r];
+        wavey_cuda_plan *pl = nullptr;
+        st = plan_create(ctx, j.grid, j.sources, j.n_sources, j.signals, j.signal_stride, j.steps, j.receivers, j.n_recv,
+                         j.freqs, j.nf, precision, want_ir, &pl, false);
+        if (st) {
+            std::string msg = ctx->err;
+            ctx->fail(st, "room %zu: %s", r, msg.c_str());
+            return bail(st);
+        }
+        rm->plans.push_back(pl);
+        rm->max_steps = std::max<int64_t>(rm->max_steps, pl->steps);
+    }
+    cudaError_t e = cudaMalloc(&rm->base, sizeof(long long));
+    if (e != cudaSuccess) return bail(ctx->cuda(e, "step counter"));
+    for (wavey_cuda_plan *pl : rm->plans) pl->base = rm->base;
+    st = precision == WAVEY_FP64 ? rooms_table<double, true>(rm) : rooms_table<float, false>(rm);
+    if (st) return bail(st);
+    for (cudaEvent_t *ev : {&rm->ev_a, &rm->ev_b, &rm->ev_t0, &rm->ev_t1})
+        if ((st = ctx->cuda(cudaEventCreate(ev), "event create"))) return bail(st);
+    if ((st = rooms_graph(rm))) return bail(st);
+    *out = rm;
+    return WAVEY_OK;
+}
+
+int rooms_run(wavey_cuda_rooms *rm, const volatile int32_t *cancel, void (*progress)(double, void *), void *user,
+              wavey_run_stats *stats) {
+    wavey_cuda_ctx *ctx = rm->ctx;
+    cudaStream_t s = ctx->stream;
+    int st;
+    cudaEventRecord(rm->ev_t0, s);
+    for (wavey_cuda_plan *pl : rm->plans)
+        if ((st = plan_reset(pl))) return st;
+    if ((st = ctx->cuda(cudaMemsetAsync(rm->base, 0, sizeof(long long), s), "memset"))) return st;
+    const int64_t chunks = (rm->max_steps + wk::RING - 1) / wk::RING;
+    double step_ms = 0.0;
+    for (int64_t c = 0; c < chunks; c++) {
+        if (cancel && *cancel) {
+            cudaStreamSynchronize(s);
+            return WAVEY_CANCELLED;
+        }
+        if ((st = ctx->cuda(cudaGraphLaunch(rm->graph, s), "graph launch"))) return st;
+        if (stats || cancel || progress) {
+            if ((st = ctx->cuda(cudaEventSynchronize(rm->ev_b), "chunk wait"))) return st;
+            if (stats) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, rm->ev_a, rm->ev_b);
+                step_ms += ms;
+            }
+        }
+        if (progress) progress((double)std::min<int64_t>((c + 1) * wk::RING, rm->max_steps) / (double)rm->max_steps, user);
+    }
+    cudaEventRecord(rm->ev_t1, s);
+    if ((st = ctx->cuda(cudaStreamSynchronize(s), "run"))) return st;
+    for (size_t r = 0; r < rm->plans.size(); r++) {
+        int err_word = 0;
+        if ((st = ctx->cuda(cudaMemcpy(&err_word, rm->plans[r]->err, sizeof(int), cudaMemcpyDeviceToHost), "error word")))
+            return st;
+        if (err_word) return ctx->fail(WAVEY_E_DEVICE, "room %zu: a kernel reported error %d", r, err_word);
+        rm->plans[r]->ran = true;
+    }
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, rm->ev_t0, rm->ev_t1);
+        stats->total_ms = ms;
+        stats->step_ms = step_ms;
+        stats->step_launches = chunks * wk::RING;
+        stats->chunks = chunks;
+    }
+    rm->ran = true;
     return WAVEY_OK;
 }
 
@@ -1058,4 +1251,63 @@ int wavey_cuda_fdtd_run(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey
                                      ir_out, cancel, progress, user);
 }
 
+int wavey_cuda_rooms_create(wavey_cuda_ctx *ctx, const wavey_room_job *jobs, size_t n_jobs, int32_t precision,
+                            int32_t want_ir, wavey_cuda_rooms **out) {
+    if (!ctx) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return rooms_create(ctx, jobs, n_jobs, precision, want_ir, out);
+}
+
+int wavey_cuda_rooms_run(wavey_cuda_rooms *rooms, const volatile int32_t *cancel, void (*progress)(double, void *),
+                         void *user, wavey_run_stats *stats) {
+    if (!rooms) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(rooms->ctx->mu);
+    cudaSetDevice(rooms->ctx->device);
+    return rooms_run(rooms, cancel, progress, user, stats);
+}
+
+int wavey_cuda_rooms_read(wavey_cuda_rooms *rooms, size_t room, double *out, double *ir_out) {
+    if (!rooms) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(rooms->ctx->mu);
+    cudaSetDevice(rooms->ctx->device);
+    if (room >= rooms->plans.size()) return rooms->ctx->fail(WAVEY_E_INVALID, "room %zu out of range", room);
+    return plan_read(rooms->plans[room], out, ir_out);
+}
+
+int wavey_cuda_rooms_info(const wavey_cuda_rooms *rooms, size_t room, wavey_plan_info *info) {
+    if (!rooms || room >= rooms->plans.size()) return WAVEY_E_INVALID;
+    int st = wavey_cuda_plan_info(rooms->plans[room], info);
+    info->graph_kernels = rooms->graph_kernels;
+    return st;
+}
+
+void wavey_cuda_rooms_destroy(wavey_cuda_rooms *rooms) {
+    if (!rooms) return;
+    wavey_cuda_ctx *ctx = rooms->ctx;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    delete rooms;
+}
+
+int wavey_cuda_fdtd_run_rooms(wavey_cuda_ctx *ctx, const wavey_room_job *jobs, size_t n_jobs, int32_t precision,
+                              const volatile int32_t *cancel, void (*progress)(double, void *), void *user) {
+    if (!ctx) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    bool want_ir = false;
+    for (size_t r = 0; jobs && r < n_jobs; r++) want_ir = want_ir || jobs[r].ir_out;
+    wavey_cuda_rooms *rm = nullptr;
+    int st = rooms_create(ctx, jobs, n_jobs, precision, want_ir, &rm);
+    if (st) return st;
+    st = rooms_run(rm, cancel, progress, user, nullptr);
+    for (size_t r = 0; st == WAVEY_OK && r < n_jobs; r++)
+        if (jobs[r].out || jobs[r].ir_out) st = plan_read(rm->plans[r], jobs[r].out, jobs[r].ir_out);
+    cudaStreamSynchronize(ctx->stream);
+    delete rm;
+    return st;
+}
+
 }  // extern "C"
+

@@ -9,6 +9,10 @@ configurations (no measured rooms or speaker data are needed).
                   63..1000 Hz fitted to the boundary filter form, one cardioid
                   (monopole + 3 dipoles = 4 right-hand sides), 64 receivers
                   plus a 1.2 m cut plane at 0.25 m spacing, 1.0 s (~7 M cells)
+  rooms_batch     room_small's room with 32 speakers (seeded monopoles and
+                  cardioids, one right-hand side or four each) plus four
+                  shoeboxes of U(5,25) x U(4,20) x U(3,10) m at 250 Hz with one
+                  monopole each, all in one launch per step
   room_hall       40 x 25 x 15 m with 12 pillars and a stepped balcony at
                   1 kHz (~370 M cells), 8 materials
 
@@ -181,3 +185,41 @@ def octave_levels(transfer: np.ndarray, freqs: np.ndarray, centres) -> np.ndarra
         sel = (freqs >= lo) & (freqs < hi)
         out.append(10.0 * np.log10(np.mean(np.abs(transfer[..., sel]) ** 2, axis=-1)))
     return np.stack(out, axis=-1)
+
+
+def rooms_batch(seed: int = 3, speakers: int = 32, extra_rooms: int = 4):
+    """The multi-room batch: a list of Scenes sharing one launch per step."""
+    rng = np.random.default_rng(seed)
+    fc = 250.0
+    first = room_small(seed=1)
+    g = first.grid
+    sources, kinds = [], []
+    for _ in range(speakers):
+        pos = _random_points(rng, first.room, 1, margin=2 * g.dx + 0.2)[0]
+        if rng.uniform() < 0.5:
+            sources.append(g.taps_at(pos))
+            kinds.append("monopole")
+        else:
+            comps = source_components(g, g.nearest_air(pos), 1)
+            if comps is None:
+                sources.append(g.taps_at(pos))
+                kinds.append("monopole")
+            else:
+                sources.extend(comps)
+                kinds.append("cardioid")
+    first.sources = sources
+    first.name = f"room_small_{speakers}spk"
+    first.notes = dict(first.notes, speakers=kinds)
+    scenes = [first]
+    for r in range(extra_rooms):
+        dims = (float(rng.uniform(5, 25)), float(rng.uniform(4, 20)), float(rng.uniform(3, 10)))
+        room = BoxRoom(*dims)
+        mats = [Material(id=f"r{r}a{i}", absorption=Spectrum(float(rng.uniform(0.05, 0.4)))) for i in range(6)]
+        fits = fit_surfaces(mats, (20.0, fc * math.sqrt(2.0)))
+        gr = FdtdGrid.build(room, fits, C_AIR, fc, 10.0)
+        src = _random_points(rng, room, 1, margin=1.0)[0]
+        rx = [gr.nearest_air(p) for p in _random_points(rng, room, 8)]
+        steps = math.ceil(0.5 / gr.dt)
+        scenes.append(Scene(f"shoebox_{r}", room, gr, fits, [gr.taps_at(src)], source_signal(fc, gr.dt, steps), rx,
+                            wave_freqs(fc), fc, notes={"dims": dims}))
+    return scenes
