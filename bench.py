@@ -157,13 +157,21 @@ def profiled_traffic(workload: str):
     return float(m.group(1)) if m else None
 
 
-def make_scene(workload: str, seed: int):
+def make_scene(workload: str, seed: int, args=None):
     from wavey_gb300 import workloads as W
 
     if workload == "room_pillars":
         return W.room_pillars(seed=2)
     if workload == "room_small":
         return W.room_small(seed=1)
+    if workload == "room_hall":
+        # 376 M cells: a full 2 s run is 34,641 steps; the throughput of a step
+        # does not change along the run, so a bounded prefix is timed.
+        sc = W.room_hall(speakers=args.hall_speakers if args else 16)
+        steps = args.hall_steps if args else 384
+        sc.signal = sc.signal[:steps]
+        sc.notes["steps_timed"] = f"first {steps} of {W.math.ceil(2.0 / sc.grid.dt)} steps"
+        return sc
     raise SystemExit(f"unknown workload {workload}")
 
 
@@ -187,7 +195,7 @@ def run_reference(args, rank, world):
     from oracle import build as obuild
 
     obuild.build()
-    scene = make_scene(args.workload, 0)
+    scene = make_scene(args.workload, 0, args)
     sample = args.sample_steps
     for _ in range(args.warmup):
         cpu_sample(scene, sample)
@@ -226,14 +234,27 @@ def run_ours(args, rank, world):
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
-    scene = make_scene(args.workload, rank)
+    scene = make_scene(args.workload, rank, args)
     g = scene.grid
+    if args.workload == "room_hall":
+        # Memory check before allocating: fields, ring and spectra of the batch.
+        free, _total = torch.cuda.mem_get_info()
+        S_pad = -(-len(scene.sources) // 4) * 4
+        need = 2 * (-(-g.n[0] // 32) * 32) * g.n[1] * g.n[2] * S_pad * 4 * 1.15
+        if need > free:
+            raise SystemExit(f"room_hall needs about {need / 1e9:.0f} GB of device memory, {free / 1e9:.0f} GB free")
+        args.no_plain = args.no_e2e_big = True
+        args.no_accuracy = args.no_cpu = args.no_autotune = True
     S = len(scene.sources)
     b = CudaBackend(dev)
     name, sms = b.device_info()
     log(f"[rank {rank}] {name} ({sms} SMs): {scene.name} grid {g.n}, air {g.air}, {scene.steps} steps, S={S}, "
         f"{len(scene.receivers)} receivers x {len(scene.freqs)} bins")
     plan = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
+    tuned = plan.autotune() if not args.no_autotune else None
+    if tuned:
+        log(f"[rank {rank}] autotuned: rows {tuned['rows']}, rings {tuned['p_planes']}/{tuned['q_planes']}, "
+            f"z-run {tuned['zt']}: {tuned['step_us']:.1f} us/step")
     info = plan.info()
     log(f"[rank {rank}] plan: {info}")
     for _ in range(args.warmup):
@@ -258,6 +279,7 @@ def run_ours(args, rank, world):
     elapsed = max_over_ranks(total_ms / 1e3, world)
     value = updates_per_run * args.steps * world / elapsed / 1e9
     spec32 = plan.read()
+    plan.close()  # frees its device memory before the other legs allocate theirs
 
     # Roofline of the fused step kernel.
     peak, peak_kind = peaks()
@@ -279,7 +301,7 @@ def run_ours(args, rank, world):
 
     # End to end through the C-ABI with host buffers.
     e2e_times = []
-    for _ in range(args.e2e_steps):
+    for _ in range(0 if getattr(args, "no_e2e_big", False) else args.e2e_steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         b.run_batch(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
@@ -355,7 +377,9 @@ def run_ours(args, rank, world):
             "config": {"workload": scene.name, "grid": list(g.n), "air_cells": g.air, "time_steps": scene.steps,
                        "right_hand_sides": S, "receivers": len(scene.receivers), "freq_bins": len(scene.freqs),
                        "batched": True, "l2": "fields 2x%.0f MB > L2 (no flush needed)" % (info["device_bytes"] / 2e6),
-                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
+                       "autotuned": None if not tuned else {k: tuned[k] for k in ("rows", "p_planes", "q_planes", "zt",
+                                                                                  "step_us")}},
             "per_source": value / S,
             "plain": {"value": plain, "per_source": None if plain is None else plain / S,
                       "batched_over_plain": None if plain is None else value / world / plain},
@@ -391,6 +415,9 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp16", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--hall-steps", type=int, default=384)
+    ap.add_argument("--hall-speakers", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 (timing rule)")

@@ -129,6 +129,21 @@ int wavey_cuda_plan_run(wavey_cuda_plan *plan, const volatile int32_t *cancel, v
                         void *user, wavey_run_stats *stats);
 int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out);
 int wavey_cuda_plan_info(const wavey_cuda_plan *plan, wavey_plan_info *info);
+
+/* Autotuner of a plan's interior kernel (FP32 plans of at least 256 steps):
+ * every candidate shape -- tile rows (8 or 16) with ring depths, and z
+ * planes per CTA (8, 16, 32) -- runs two 128-step chunks of the plan's own
+ * grid, and the plan keeps the fastest.  result (nullable) lists the
+ * candidates' step times.  Other plans are left as they are. */
+#define WAVEY_TUNE_MAX 32
+typedef struct {
+    int32_t cfg, zt, rows, p_planes, q_planes;
+    double step_us;
+    int32_t candidates;
+    int32_t cand_cfg[WAVEY_TUNE_MAX], cand_zt[WAVEY_TUNE_MAX];
+    double cand_step_us[WAVEY_TUNE_MAX];
+} wavey_tune_result;
+int wavey_cuda_plan_autotune(wavey_cuda_plan *plan, wavey_tune_result *result);
 void wavey_cuda_plan_destroy(wavey_cuda_plan *plan);
 
 /* Several rooms in one launch per time step: the rooms' step blocks are laid

@@ -118,6 +118,18 @@ class WaveyPlanInfo(C.Structure):
     ]
 
 
+WAVEY_TUNE_MAX = 32
+
+
+class WaveyTuneResult(C.Structure):
+    _fields_ = [
+        ("cfg", C.c_int32), ("zt", C.c_int32), ("rows", C.c_int32), ("p_planes", C.c_int32), ("q_planes", C.c_int32),
+        ("step_us", C.c_double), ("candidates", C.c_int32),
+        ("cand_cfg", C.c_int32 * WAVEY_TUNE_MAX), ("cand_zt", C.c_int32 * WAVEY_TUNE_MAX),
+        ("cand_step_us", C.c_double * WAVEY_TUNE_MAX),
+    ]
+
+
 PROGRESS_FN = C.CFUNCTYPE(None, C.c_double, C.c_void_p)
 
 _host = None
@@ -204,6 +216,7 @@ def cuda() -> C.CDLL:
         "wavey_cuda_plan_read": (C.c_int, [vp, c_double_p, c_double_p]),
         "wavey_cuda_plan_info": (C.c_int, [vp, C.POINTER(WaveyPlanInfo)]),
         "wavey_cuda_plan_destroy": (None, [vp]),
+        "wavey_cuda_plan_autotune": (C.c_int, [vp, C.POINTER(WaveyTuneResult)]),
         "wavey_cuda_fdtd_run_rooms": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, cancel_p,
                                                 PROGRESS_FN, vp]),
         "wavey_cuda_rooms_create": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, C.c_int32,

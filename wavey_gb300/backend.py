@@ -313,6 +313,16 @@ class Plan:
                                                              N.ptr(irbuf, C.c_double)))
         return (out, irbuf) if self.ir else out
 
+    def autotune(self) -> dict:
+        """Times every candidate shape of the interior kernel on this plan's
+        grid and keeps the fastest (wavey_cuda_plan_autotune)."""
+        r = N.WaveyTuneResult()
+        with self._b._lock:
+            self._b._check(self._b._lib.wavey_cuda_plan_autotune(self._h, C.byref(r)))
+        return {"cfg": r.cfg, "zt": r.zt, "rows": r.rows, "p_planes": r.p_planes, "q_planes": r.q_planes,
+                "step_us": r.step_us,
+                "candidates": [(r.cand_cfg[i], r.cand_zt[i], r.cand_step_us[i]) for i in range(r.candidates)]}
+
     def info(self) -> dict:
         i = N.WaveyPlanInfo()
         self._b._lib.wavey_cuda_plan_info(self._h, C.byref(i))

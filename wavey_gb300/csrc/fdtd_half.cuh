@@ -10,13 +10,16 @@
 // from the slab maxima of the two previous levels over slabs z-1..z+1:
 //
 //     M = 8 * max(amax^n[z-1..z+1], amax^(n-1)[z-1..z+1]) + injection bound
-//     E^(n+1)[z] = e - 15 with M < 2^e.
+//     E^(n+1)[z] = max(e - shift, E_FLOOR) with M < 2^e (shift 14 by default).
 //
-// The factor 8 bounds the growth of one leapfrog step over a cell's
-// neighbourhood (|p+| <= 2|p| + |p-| + 12 l2 |p|max), and 2^15 keeps the
-// largest value below FP16's 65504.  A value outside the FP16 range anyway
-// sets the error word (the host reports WAVEY_E_DEVICE) instead of
-// saturating.  Scales (2^E and 2^-E) live in a ring of three levels, slab
+// The factor 8 bounds the growth of one leapfrog step of pressure alone over
+// a cell's neighbourhood (|p+| <= 2|p| + |p-| + 12 l2 |p|max); boundary nodes
+// can exceed it, because their branch states hold energy the pressure maxima
+// do not see, so M maps to 2^14, leaving 4 times headroom below 65504.  FP16
+// is floating point: power-of-two scaling does not change its rounding, so
+// the mapping only trades headroom against the subnormal range (values below
+// 2^-28 of M lose bits).  A value outside the FP16 range anyway sets the
+// error word (the host reports WAVEY_E_DEVICE) instead of saturating.  Scales (2^E and 2^-E) live in a ring of three levels, slab
 // maxima in a ring of three levels; half_prepare also clears the maxima slot
 // the step is about to accumulate.
 #pragma once
@@ -28,7 +31,7 @@ namespace wk {
 
 constexpr int AMAX_RING = 3;
 constexpr int SCALE_RING = 3;
-constexpr int E_FLOOR = -60;  // exponent of a slab that has held only zeros
+constexpr int E_FLOOR = -60;  // lowest slab exponent: slabs that hold only zeros or near-zeros
 constexpr int ERR_FP16_RANGE = 2;
 
 struct HalfArgs {
@@ -53,6 +56,7 @@ struct HalfArgs {
     int tiles_x, tiles_y, tiles_z, zt;
     int interior_blocks, special_blocks, record_blocks;
     float l2, lam, half_dt;
+    int shift;  // the bound M maps just below 2^shift
 };
 
 __device__ __forceinline__ float slab_max(const HalfArgs &a, long long level, int c, int z) {
@@ -83,9 +87,13 @@ __device__ __forceinline__ int slab_exponent(const HalfArgs &a, long long k, int
     if (m == 0.0f) return E_FLOOR;
     int e;
     frexpf(m, &e);
-    return e - 15;
+    // Slabs ahead of a wave front can hold FP32 subnormals; their exponent is
+    // clamped to the floor (they read back as the zeros they nearly are), which
+    // also keeps 2^E and 2^-E inside the normal FP32 range that pow2 builds.
+    return max(e - a.shift, E_FLOOR);
 }
 
+// 2^e for -126 <= e <= 127 (slab exponents stay in [E_FLOOR, 127 - 10]).
 __device__ __forceinline__ float pow2(int e) { return __int_as_float((127 + e) << 23); }
 
 // (2^E, 2^-E) of level k, slab z, chunk c.
@@ -141,7 +149,7 @@ __device__ __forceinline__ float store_h(__half *p, const Lanes<float, V> &v, fl
 #pragma unroll
     for (int l = 0; l < V; l++) {
         const float s = v.v[l] * inv;
-        if (!(fabsf(s) <= 65504.0f)) atomicExch(error, ERR_FP16_RANGE);
+        if (!(fabsf(s) <= 65504.0f) && *reinterpret_cast<volatile int *>(error) == 0) atomicExch(error, ERR_FP16_RANGE);
         h[l] = __float2half_rn(s);
         m = fmaxf(m, fabsf(v.v[l]));
     }

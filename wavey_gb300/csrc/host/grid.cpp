@@ -241,16 +241,25 @@ extern "C" int wh_grid_build(const wh_room *room, const wh_fit *fits, int32_t n_
                 g->flags[i] = fl;
             }
     // Surfaces behind the missing faces (fdtd.rs:357-363) and the slots of
-    // each boundary node (fdtd.rs:368-375), in cell order so that boundary
-    // node numbering follows the cell index as in the reference.
-    std::vector<Slot> sl;
-    std::vector<int> flist;
-    for (int64_t z = 1; z < nz - 1; z++)
+    // each boundary node (fdtd.rs:368-375).  Planes are done in parallel,
+    // then concatenated in plane order, so boundary nodes are numbered in cell
+    // order as in the reference.
+    struct PlaneNodes {
+        std::vector<uint32_t> cell, nslots;
+        std::vector<double> slots;
+        int64_t air = 0;
+    };
+    std::vector<PlaneNodes> planes(nz);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t z = 1; z < nz - 1; z++) {
+        PlaneNodes &pn = planes[z];
+        std::vector<Slot> sl;
+        std::vector<int> flist;
         for (int64_t y = 1; y < ny - 1; y++)
             for (int64_t x = 1; x < nx - 1; x++) {
                 int64_t i = g->index(x, y, z);
                 if (!air[i]) continue;
-                g->air++;
+                pn.air++;
                 uint8_t fl = g->flags[i];
                 if ((fl & 63) == 63) continue;
                 double p[3];
@@ -280,17 +289,47 @@ extern "C" int wh_grid_build(const wh_room *room, const wh_fit *fits, int32_t n_
                 }
                 boundary_slots(flist.data(), (int)flist.size(), fits, g->dt, sl);
                 if (!sl.empty()) {
-                    g->bidx[i] = (uint32_t)g->bcell.size();
-                    g->bcell.push_back((uint32_t)i);
-                    g->bstart.push_back((uint32_t)(g->slots.size() / 4));
-                    for (const Slot &s : sl) {
-                        g->slots.push_back(s.inv_d);
-                        g->slots.push_back(s.cv);
-                        g->slots.push_back(s.k);
-                        g->slots.push_back(s.w);
+                    pn.cell.push_back((uint32_t)i);
+                    pn.nslots.push_back((uint32_t)sl.size());
+                    for (const Slot &q : sl) {
+                        pn.slots.push_back(q.inv_d);
+                        pn.slots.push_back(q.cv);
+                        pn.slots.push_back(q.k);
+                        pn.slots.push_back(q.w);
                     }
                 }
             }
+    }
+    size_t n_nodes = 0, n_vals = 0;
+    for (const PlaneNodes &pn : planes) {
+        n_nodes += pn.cell.size();
+        n_vals += pn.slots.size();
+    }
+    if (n_nodes >= (size_t)WAVEY_NO_BOUNDARY) {
+        delete g;
+        return WAVEY_E_LIMIT;
+    }
+    try {
+        g->bcell.reserve(n_nodes);
+        g->bstart.reserve(n_nodes + 1);
+        g->slots.reserve(n_vals);
+    } catch (...) {
+        delete g;
+        return WAVEY_E_NOMEM;
+    }
+    for (PlaneNodes &pn : planes) {
+        g->air += pn.air;
+        size_t v = 0;
+        for (size_t k = 0; k < pn.cell.size(); k++) {
+            g->bidx[pn.cell[k]] = (uint32_t)g->bcell.size();
+            g->bcell.push_back(pn.cell[k]);
+            g->bstart.push_back((uint32_t)(g->slots.size() / 4));
+            g->slots.insert(g->slots.end(), pn.slots.begin() + v, pn.slots.begin() + v + 4 * pn.nslots[k]);
+            v += 4 * pn.nslots[k];
+        }
+        PlaneNodes().cell.swap(pn.cell);
+        std::vector<double>().swap(pn.slots);
+    }
     g->bstart.push_back((uint32_t)(g->slots.size() / 4));
     *out = g;
     return WAVEY_OK;

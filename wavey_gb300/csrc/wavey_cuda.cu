@@ -131,6 +131,7 @@ struct wavey_cuda_plan {
     size_t field_elem = 4;  // bytes of a stored field value (2 in FP16 storage)
     unsigned int *amax = nullptr;  // FP16 storage: slab maxima ring
     float2 *scale = nullptr;       // FP16 storage: slab scale ring
+    int fp16_shift = 14;           // FP16 storage: the slab bound maps just below 2^shift
     float *wmax = nullptr;         // FP16 storage: sum |tap weight| per source
     // launch geometry
     int tiles_x = 0, tiles_y = 0, tiles_z = 0;
@@ -413,6 +414,7 @@ void launch_step_half(wavey_cuda_plan *pl, int t, int parity) {
     a.l2 = (float)(COURANT * COURANT);
     a.lam = (float)COURANT;
     a.half_dt = 0.5f * (float)pl->dt;
+    a.shift = pl->fp16_shift;
     const int prep = (int)((pl->chunks * pl->nz + wk::BLOCK - 1) / wk::BLOCK);
     wk::half_prepare<V><<<prep, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
     const int blocks = pl->interior_blocks + pl->special_blocks + pl->record_blocks;
@@ -533,6 +535,42 @@ int upload_typed(wavey_cuda_plan *pl, void **out, const std::vector<double> &src
     if (st) return st;
     // The staging vector dies here: wait for the copy.
     return pl->ctx->cuda(cudaStreamSynchronize(pl->ctx->stream), "upload sync");
+}
+
+// Shape of the TMA interior kernel: tile rows and ring depths (TMA_CFGS[cfg])
+// and the z planes each CTA marches (zt).  Encodes the tensor maps, whose
+// boxes depend on the tile rows, and sizes the grid.
+int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    EncodeTiled enc = encode_tiled();
+    if (!enc) return ctx->fail(WAVEY_E_CUDA, "the driver lacks cuTensorMapEncodeTiled");
+    const int64_t V = pl->V, nx = pl->nx, ny = pl->ny, nz = pl->nz;
+    const cuuint64_t dims[4] = {(cuuint64_t)(nx * V), (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)pl->chunks};
+    const cuuint64_t strides[3] = {(cuuint64_t)(pl->nxp * V * 4), (cuuint64_t)(pl->nxp * ny * V * 4),
+                                   (cuuint64_t)(pl->cells_p * V * 4)};
+    const int rows = TMA_CFGS[cfg].rows;
+    const cuuint32_t box_p[4] = {(cuuint32_t)wk::TMA_P_ROW, (cuuint32_t)(rows + 2), 1, 1};
+    const cuuint32_t box_q[4] = {(cuuint32_t)wk::TMA_ROW_FLOATS, (cuuint32_t)rows, 1, 1};
+    const cuuint32_t unit[4] = {1, 1, 1, 1};
+    for (int k = 0; k < 2; k++) {
+        CUresult r1 = enc(&pl->tm_p[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k], dims, strides, box_p, unit,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        CUresult r2 = enc(&pl->tm_q[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k ^ 1], dims, strides, box_q, unit,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS)
+            return ctx->fail(WAVEY_E_CUDA, "tensor map encoding failed (%d, %d)", (int)r1, (int)r2);
+    }
+    pl->tma_cfg = cfg;
+    pl->tma_zt = zt;
+    pl->tma_tiles_x = (int)((nx + (wk::TMA_ROW_FLOATS / V) - 1) / (wk::TMA_ROW_FLOATS / V));
+    pl->tma_tiles_y = (int)((ny - 2 + rows - 1) / rows);
+    pl->tma_tiles_z = (int)((nz - 2 + zt - 1) / zt);
+    const int64_t tb = (int64_t)pl->tma_tiles_x * pl->tma_tiles_y * pl->tma_tiles_z * pl->chunks;
+    if (tb >= (1ll << 31)) return ctx->fail(WAVEY_E_LIMIT, "launch grid too large");
+    pl->tma_blocks = (int)tb;
+    return WAVEY_OK;
 }
 
 // standalone: a plan that runs by itself (TMA interior path where it
@@ -764,6 +802,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if ((st = upload(pl, &pl->wmax, wm.data(), wm.size() * 4))) return bail(st);
         if ((st = alloc(pl, &pl->amax, (size_t)wk::AMAX_RING * pl->chunks * nz * sizeof(unsigned int)))) return bail(st);
         if ((st = alloc(pl, &pl->scale, (size_t)wk::SCALE_RING * pl->chunks * nz * sizeof(float2)))) return bail(st);
+        pl->fp16_shift = env_int("WAVEY_FP16_SHIFT", 14, 8, 15);
         if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
     }
     if ((st = upload(pl, &pl->recv, recv_p.data(), recv_p.size() * 4))) return bail(st);
@@ -787,35 +826,8 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if ((st = ctx->cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event create"))) return bail(st);
     if ((st = alloc(pl, &pl->err, sizeof(int)))) return bail(st);
     if (standalone && precision == WAVEY_FP32 && tma_selected()) {
-        EncodeTiled enc = encode_tiled();
-        if (!enc) return bail(ctx->fail(WAVEY_E_CUDA, "the driver lacks cuTensorMapEncodeTiled"));
-        const int V = pl->V;
-        const cuuint64_t dims[4] = {(cuuint64_t)(nx * V), (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)pl->chunks};
-        const cuuint64_t strides[3] = {(cuuint64_t)(pl->nxp * V * 4), (cuuint64_t)(pl->nxp * ny * V * 4),
-                                       (cuuint64_t)(pl->cells_p * V * 4)};
-        pl->tma_cfg = env_int("WAVEY_TMA_CFG", 0, 0, TMA_NCFG - 1);
-        const int rows = TMA_CFGS[pl->tma_cfg].rows;
-        const cuuint32_t box_p[4] = {(cuuint32_t)wk::TMA_P_ROW, (cuuint32_t)(rows + 2), 1, 1};
-        const cuuint32_t box_q[4] = {(cuuint32_t)wk::TMA_ROW_FLOATS, (cuuint32_t)rows, 1, 1};
-        const cuuint32_t unit[4] = {1, 1, 1, 1};
-        for (int k = 0; k < 2; k++) {
-            CUresult r1 = enc(&pl->tm_p[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k], dims, strides, box_p, unit,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            CUresult r2 = enc(&pl->tm_q[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k ^ 1], dims, strides, box_q, unit,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS)
-                return bail(ctx->fail(WAVEY_E_CUDA, "tensor map encoding failed (%d, %d)", (int)r1, (int)r2));
-        }
-        pl->tma_zt = env_int("WAVEY_TMA_ZT", 16, 1, 4096);
-        pl->tma_tiles_x = (int)((nx + (wk::TMA_ROW_FLOATS / V) - 1) / (wk::TMA_ROW_FLOATS / V));
-        pl->tma_tiles_y = (int)((ny - 2 + rows - 1) / rows);
-        pl->tma_tiles_z = (int)((nz - 2 + pl->tma_zt - 1) / pl->tma_zt);
-        const int64_t tb = (int64_t)pl->tma_tiles_x * pl->tma_tiles_y * pl->tma_tiles_z * pl->chunks;
-        if (tb >= (1ll << 31)) return bail(ctx->fail(WAVEY_E_LIMIT, "launch grid too large"));
-        pl->tma_blocks = (int)tb;
-
+        if ((st = tma_shape(pl, env_int("WAVEY_TMA_CFG", 0, 0, TMA_NCFG - 1), env_int("WAVEY_TMA_ZT", 16, 1, 4096))))
+            return bail(st);
         cudaError_t e = tma_attrs<1>();
         if (e == cudaSuccess) e = tma_attrs<2>();
         if (e == cudaSuccess) e = tma_attrs<4>();
@@ -1115,6 +1127,61 @@ int rooms_run(wavey_cuda_rooms *rm, const volatile int32_t *cancel, void (*progr
     return WAVEY_OK;
 }
 
+
+// The autotuner: every candidate shape of the TMA interior kernel runs two
+// 128-step chunks of this plan's own grid; the fastest step span wins and
+// the plan keeps it.  Needs a TMA plan with at least 256 steps.
+int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    if (res) *res = wavey_tune_result{};
+    if (!pl->tma || pl->steps < 2 * wk::RING || !pl->graph) return WAVEY_OK;
+    static const int ZTS[] = {8, 16, 32};
+    int best_cfg = pl->tma_cfg, best_zt = pl->tma_zt, n = 0, st;
+    double best = 1e30;
+    cudaStream_t s = ctx->stream;
+    for (int cfg = 0; cfg < TMA_NCFG; cfg++)
+        for (int zt : ZTS) {
+            if ((st = tma_shape(pl, cfg, zt))) return st;
+            cudaGraphExecDestroy(pl->graph);
+            pl->graph = nullptr;
+            if ((st = build_graph(pl))) return st;
+            if ((st = plan_reset(pl))) return st;
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; rep++) {
+                if ((st = ctx->cuda(cudaGraphLaunch(pl->graph, s), "graph launch"))) return st;
+                if ((st = ctx->cuda(cudaEventSynchronize(pl->ev_b), "tune wait"))) return st;
+                cudaEventElapsedTime(&ms, pl->ev_a, pl->ev_b);  // the second chunk's span counts
+            }
+            const double us = 1e3 * ms / wk::RING;
+            if (res && n < WAVEY_TUNE_MAX) {
+                res->cand_cfg[n] = cfg;
+                res->cand_zt[n] = zt;
+                res->cand_step_us[n] = us;
+            }
+            n++;
+            if (us < best) {
+                best = us;
+                best_cfg = cfg;
+                best_zt = zt;
+            }
+        }
+    if ((st = tma_shape(pl, best_cfg, best_zt))) return st;
+    cudaGraphExecDestroy(pl->graph);
+    pl->graph = nullptr;
+    if ((st = build_graph(pl))) return st;
+    if ((st = ctx->cuda(cudaStreamSynchronize(s), "tune"))) return st;
+    if (res) {
+        res->cfg = best_cfg;
+        res->zt = best_zt;
+        res->rows = TMA_CFGS[best_cfg].rows;
+        res->p_planes = TMA_CFGS[best_cfg].np;
+        res->q_planes = TMA_CFGS[best_cfg].nq;
+        res->step_us = best;
+        res->candidates = std::min(n, WAVEY_TUNE_MAX);
+    }
+    return WAVEY_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1187,6 +1254,13 @@ int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out) {
     std::lock_guard<std::mutex> lock(plan->ctx->mu);
     cudaSetDevice(plan->ctx->device);
     return plan_read(plan, out, ir_out);
+}
+
+int wavey_cuda_plan_autotune(wavey_cuda_plan *plan, wavey_tune_result *result) {
+    if (!plan) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(plan->ctx->mu);
+    cudaSetDevice(plan->ctx->device);
+    return plan_autotune(plan, result);
 }
 
 int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {

@@ -223,3 +223,59 @@ def rooms_batch(seed: int = 3, speakers: int = 32, extra_rooms: int = 4):
         scenes.append(Scene(f"shoebox_{r}", room, gr, fits, [gr.taps_at(src)], source_signal(fc, gr.dt, steps), rx,
                             wave_freqs(fc), fc, notes={"dims": dims}))
     return scenes
+
+
+def plane_points_axis(room, axis: str, offset: float, spacing: float):
+    """Inside points of a vertical cut plane (receivers.rs:118-140): axis "x"
+    is x = offset (u = y, v = z), axis "y" is y = offset (u = x, v = z)."""
+    if axis == "x":
+        ulo, uhi = room.y0, room.y1
+    else:
+        ulo, uhi = room.x0, room.x1
+    vlo, vhi = 0.0, room.height
+    nu = max(1, math.ceil((uhi - ulo) / spacing))
+    nv = max(1, math.ceil((vhi - vlo) / spacing))
+    u0 = (ulo + uhi) / 2.0 - (nu - 1.0) / 2.0 * spacing
+    v0 = (vlo + vhi) / 2.0 - (nv - 1.0) / 2.0 * spacing
+    pts = []
+    for iv in range(nv):
+        for iu in range(nu):
+            u, v = u0 + iu * spacing, v0 + iv * spacing
+            p = (offset, u, v) if axis == "x" else (u, offset, v)
+            if room.contains(p):
+                pts.append(p)
+    return pts
+
+
+def room_hall(seed: int = 5, speakers: int = 16, duration: float = 2.0, crossover: float = 1000.0,
+              n_mics: int = 256, plane_spacing: float = 0.25) -> Scene:
+    """40 x 25 x 15 m hall with 12 pillars and a stepped balcony (three
+    absorbing steps along the back wall), eight fitted materials, directional
+    speakers (monopole + 3 dipoles each), 256 mics and three cut planes."""
+    rng = np.random.default_rng(seed)
+    fc = crossover
+    pillars = _pillars(rng, 12, 40.0, 25.0, gap=2.0, margin=2.0)
+    z0 = float(rng.uniform(5.0, 6.0))
+    blocks = [(1.0, 19.0, z0, 39.0, 25.0, z0 + 0.4), (1.0, 21.0, z0 + 0.4, 39.0, 25.0, z0 + 0.8),
+              (1.0, 23.0, z0 + 0.8, 39.0, 25.0, z0 + 1.2)]
+    room = BoxRoom(40.0, 25.0, 15.0, pillars=pillars, blocks=blocks)
+    mats = _materials(rng, 8)
+    assign = [mats[int(k)] for k in rng.integers(0, 8, room.n_surfaces)]
+    fits = fit_surfaces(assign, (20.0, fc * math.sqrt(2.0)))
+    g = FdtdGrid.build(room, fits, C_AIR, fc, 10.0)
+    sources = []
+    for _ in range(speakers):
+        for _try in range(100):
+            pos = _random_points(rng, room, 1, margin=2.0)[0]
+            comps = source_components(g, g.nearest_air(pos), 1)
+            if comps is not None:
+                sources.extend(comps)
+                break
+    mics = [g.nearest_air(p) for p in _random_points(rng, room, n_mics)]
+    planes = (plane_points(room, 1.2, plane_spacing) + plane_points(room, z0 + 1.2 + 1.2, plane_spacing)
+              + plane_points_axis(room, "y", 12.5, plane_spacing))
+    rx = mics + [g.nearest_air(p) for p in planes]
+    steps = math.ceil(duration / g.dt)
+    return Scene("room_hall", room, g, fits, sources, source_signal(fc, g.dt, steps), rx, wave_freqs(fc), fc,
+                 notes={"seed": seed, "pillars": len(pillars), "balcony_z": z0, "speakers": speakers,
+                        "mics": len(mics), "plane_points": len(planes)})
