@@ -1,0 +1,61 @@
+"""The multi-GPU form is replicas: each rank runs its own right-hand sides on
+its own copy of the grid with no exchange on the data path; the benchmark
+only synchronises ranks around the timed region and takes the slowest.
+That host logic runs here as two gloo ranks on the CPU."""
+from __future__ import annotations
+
+import os
+import socket
+import sys
+from pathlib import Path
+
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank), WAVEY_BENCH_GLOO="1")
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    r, w = bench.dist_init()
+    bench.barrier(w)
+    slowest = bench.max_over_ranks(1.0 + r, w)  # rank r "took" 1 + r seconds
+    q.put((r, w, slowest))
+    dist.destroy_process_group()
+
+
+def test_two_replicas_agree_on_the_slowest_rank():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+    assert all(p.exitcode == 0 for p in procs)
+    res = sorted(q.get() for _ in range(2))
+    assert res == [(0, 2, 2.0), (1, 2, 2.0)]
+
+
+def test_reference_arm_runs_on_rank_zero_only():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class A:
+        workload, warmup, steps, sample_steps = "room_small", 3, 1, 5
+
+    # Rank 1 returns at once with no output; rank 0's work is tested by the
+    # bench itself.
+    assert bench.run_reference(A(), 1, 2) is None
