@@ -38,7 +38,7 @@ struct HalfArgs {
     const __half *cur;         // p^n     [chunks][cells_p][V]
     __half *nxt;               // p^(n-1) in, p^(n+1) out
     const uint32_t *interior;
-    const uint32_t *sp_cell, *sp_meta, *sp_slot0, *sp_tap;
+    const uint4 *sp;           // [n_special] {cell, meta, first slot, tap row}
     const float *slots;        // [n_slots][4]
     float *su, *sg;            // [chunks][n_slots][V]
     const float *tapw;         // [n_tap_rows][lanes_total]
@@ -237,8 +237,9 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step_half(HalfArgs a, int t) {
         if (k >= (long long)a.n_special * a.chunks) return;
         const int c = (int)(k / a.n_special);
         k -= (long long)c * a.n_special;
-        const long long cell = a.sp_cell[k];
-        const uint32_t m = a.sp_meta[k];
+        const uint4 rec = __ldg(a.sp + k);
+        const long long cell = rec.x;
+        const uint32_t m = rec.y;
         const int z = (int)(cell / nxy);
         const __half *P = a.cur + (long long)c * a.cells_p * V;
         __half *Q = a.nxt + (long long)c * a.cells_p * V;
@@ -268,7 +269,7 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step_half(HalfArgs a, int t) {
 #pragma unroll
             for (int l = 0; l < V; l++) next.v[l] = radd(rsub(rmul(2.0f, pc.v[l]), pp.v[l]), lap.v[l]);
         } else {
-            const long long j0 = a.sp_slot0[k];
+            const long long j0 = rec.z;
             float *SU = a.su + (long long)c * a.n_slots * V;
             float *SG = a.sg + (long long)c * a.n_slots * V;
             float s1 = 0.0f;
@@ -311,7 +312,7 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step_half(HalfArgs a, int t) {
                 store<float, V>(SG + j * V, g);
             }
         }
-        const uint32_t tap = a.sp_tap[k];
+        const uint32_t tap = rec.w;
         if (tap != NO_TAP) {
 #pragma unroll
             for (int l = 0; l < V; l++) {

@@ -113,10 +113,8 @@ struct StepArgs {
     const T *cur;              // p^n        [chunks][cells_p][V]
     T *nxt;                    // p^{n-1} in, p^{n+1} out
     const uint32_t *interior;  // [nz][ny][nxw] one bit per padded cell
-    const uint32_t *sp_cell;   // [n_special] padded cell index, ascending
-    const uint32_t *sp_meta;   // bits 0-5 air-neighbour flags, bits 6-10 slot count
-    const uint32_t *sp_slot0;  // first slot of the node
-    const uint32_t *sp_tap;    // tap row or NO_TAP
+    const uint4 *sp;           // [n_special] {padded cell (ascending), meta, first slot, tap row or NO_TAP};
+                               // meta: bits 0-5 air-neighbour flags, bits 6-10 slot count
     const T *slots;            // [n_slots][4] inv_d, cv, k, w
     T *su, *sg;                // [chunks][n_slots][V] branch velocity u and its integral g
     const T *tapw;             // [n_tap_rows][lanes_total] merged tap weight per source
@@ -155,18 +153,60 @@ __device__ __forceinline__ Lanes<T, V> interior_update(const Lanes<T, V> &c, con
 }
 
 // One special cell k of chunk c at step n (the special role of fdtd_step).
+// The cell's loads are issued together before any arithmetic -- its
+// neighbours, and the constants and branch states of up to SLOT_REGS slots,
+// kept in registers for both passes of the boundary solve -- because the
+// boundary solve is otherwise a chain of dependent loads per cell.
+constexpr int SLOT_REGS = 3;  // beta0 + two branches: the usual node
+
+template <class T, int V>
+struct SlotRegs {
+    T inv_d, cv, kb, w;
+    Lanes<T, V> u, g;
+};
+
+template <class T, int V>
+__device__ __forceinline__ void load_slot(const StepArgs<T> &a, const T *SU, const T *SG, long long j, SlotRegs<T, V> &r) {
+    if constexpr (sizeof(T) == 4) {
+        const float4 c = __ldg(reinterpret_cast<const float4 *>(a.slots) + j);
+        r.inv_d = c.x, r.cv = c.y, r.kb = c.z, r.w = c.w;
+    } else {
+        const double2 c0 = __ldg(reinterpret_cast<const double2 *>(a.slots) + 2 * j);
+        const double2 c1 = __ldg(reinterpret_cast<const double2 *>(a.slots) + 2 * j + 1);
+        r.inv_d = c0.x, r.cv = c0.y, r.kb = c1.x, r.w = c1.y;
+    }
+    r.u = load<T, V, false>(SU + j * V);
+    r.g = load<T, V, false>(SG + j * V);
+}
+
 template <class T, int V, bool RUST_ORDER>
 __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, long long n) {
     const long long nxy = (long long)a.nxp * a.ny;
     const int c = (int)(k / a.n_special);
     k -= (long long)c * a.n_special;
-    const long long cell = a.sp_cell[k];
-    const uint32_t m = a.sp_meta[k];
+    const uint4 rec = __ldg(a.sp + k);
+    const long long cell = rec.x;
+    const uint32_t m = rec.y;
+    const long long j0 = rec.z;
+    const uint32_t tap = rec.w;
     const T *P = a.cur + (long long)c * a.cells_p * V;
     T *Q = a.nxt + (long long)c * a.cells_p * V;
+    const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
+    T *SU = a.su + (long long)c * a.n_slots * V;
+    T *SG = a.sg + (long long)c * a.n_slots * V;
+    // All loads first.
     const Lanes<T, V> pc = load<T, V, true>(P + cell * V);
     const Lanes<T, V> pp = load<T, V, false>(Q + cell * V);
     const long long offs[6] = {-1, 1, -(long long)a.nxp, (long long)a.nxp, -nxy, nxy};
+    Lanes<T, V> nb[6];
+#pragma unroll
+    for (int d = 0; d < 6; d++)
+        if ((m >> d) & 1u) nb[d] = load<T, V, true>(P + (cell + offs[d]) * V);
+    SlotRegs<T, V> sr[SLOT_REGS];
+#pragma unroll
+    for (int q = 0; q < SLOT_REGS; q++)
+        if (q < ns) load_slot<T, V>(a, SU, SG, j0 + q, sr[q]);
+    // The laplacian over air neighbours in the -x,+x,-y,+y,-z,+z order.
     Lanes<T, V> sum;
 #pragma unroll
     for (int l = 0; l < V; l++) sum.v[l] = T(0);
@@ -174,61 +214,65 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
 #pragma unroll
     for (int d = 0; d < 6; d++) {
         if ((m >> d) & 1u) {
-            Lanes<T, V> nb = load<T, V, true>(P + (cell + offs[d]) * V);
 #pragma unroll
-            for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb.v[l]);
+            for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb[d].v[l]);
             kk = radd(kk, T(1));
         }
     }
     Lanes<T, V> lap, next;
 #pragma unroll
     for (int l = 0; l < V; l++) lap.v[l] = rmul(a.l2, rsub(sum.v[l], rmul(kk, pc.v[l])));
-    const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
     const T half = T(0.5), two = T(2), one = T(1);
     if (ns == 0) {
 #pragma unroll
         for (int l = 0; l < V; l++) next.v[l] = radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]);
     } else {
-        const long long j0 = a.sp_slot0[k];
-        T *SU = a.su + (long long)c * a.n_slots * V;
-        T *SG = a.sg + (long long)c * a.n_slots * V;
         T s1 = T(0);
         Lanes<T, V> s2;
 #pragma unroll
         for (int l = 0; l < V; l++) s2.v[l] = T(0);
         for (int q = 0; q < ns; q++) {
-            const long long j = j0 + q;
-            const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
-            const Lanes<T, V> u = load<T, V, false>(SU + j * V);
-            const Lanes<T, V> g = load<T, V, false>(SG + j * V);
+            SlotRegs<T, V> r;
+            if (q < SLOT_REGS) {
+#pragma unroll
+                for (int i = 0; i < SLOT_REGS; i++)
+                    if (i == q) r = sr[i];
+            } else {
+                load_slot<T, V>(a, SU, SG, j0 + q, r);
+            }
 #pragma unroll
             for (int l = 0; l < V; l++) {
-                T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
-                s2.v[l] = RUST_ORDER ? radd(s2.v[l], rsub(e, u.v[l])) : rsub(radd(s2.v[l], e), u.v[l]);
+                T e = rmul(radd(radd(rsub(rmul(r.cv, r.u.v[l]), rmul(r.kb, r.g.v[l])), rmul(half, pc.v[l])), rmul(r.w, pp.v[l])),
+                           r.inv_d);
+                s2.v[l] = RUST_ORDER ? radd(s2.v[l], rsub(e, r.u.v[l])) : rsub(radd(s2.v[l], e), r.u.v[l]);
             }
-            s1 = radd(s1, rmul(rsub(half, w), inv_d));
+            s1 = radd(s1, rmul(rsub(half, r.w), r.inv_d));
         }
         const T den = radd(one, rmul(a.lam, s1));
 #pragma unroll
         for (int l = 0; l < V; l++)
             next.v[l] = rdiv(rsub(radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]), rmul(a.lam, s2.v[l])), den);
         for (int q = 0; q < ns; q++) {
-            const long long j = j0 + q;
-            const T inv_d = a.slots[4 * j], cv = a.slots[4 * j + 1], kb = a.slots[4 * j + 2], w = a.slots[4 * j + 3];
-            Lanes<T, V> u = load<T, V, false>(SU + j * V);
-            Lanes<T, V> g = load<T, V, false>(SG + j * V);
+            SlotRegs<T, V> r;
+            if (q < SLOT_REGS) {
+#pragma unroll
+                for (int i = 0; i < SLOT_REGS; i++)
+                    if (i == q) r = sr[i];
+            } else {
+                load_slot<T, V>(a, SU, SG, j0 + q, r);
+            }
 #pragma unroll
             for (int l = 0; l < V; l++) {
-                T e = rmul(radd(radd(rsub(rmul(cv, u.v[l]), rmul(kb, g.v[l])), rmul(half, pc.v[l])), rmul(w, pp.v[l])), inv_d);
-                T un = radd(rmul(rmul(rsub(half, w), inv_d), next.v[l]), e);
-                g.v[l] = radd(g.v[l], rmul(a.half_dt, radd(un, u.v[l])));
-                u.v[l] = un;
+                T e = rmul(radd(radd(rsub(rmul(r.cv, r.u.v[l]), rmul(r.kb, r.g.v[l])), rmul(half, pc.v[l])), rmul(r.w, pp.v[l])),
+                           r.inv_d);
+                T un = radd(rmul(rmul(rsub(half, r.w), r.inv_d), next.v[l]), e);
+                r.g.v[l] = radd(r.g.v[l], rmul(a.half_dt, radd(un, r.u.v[l])));
+                r.u.v[l] = un;
             }
-            store<T, V>(SU + j * V, u);
-            store<T, V>(SG + j * V, g);
+            store<T, V>(SU + (j0 + q) * V, r.u);
+            store<T, V>(SG + (j0 + q) * V, r.g);
         }
     }
-    const uint32_t tap = a.sp_tap[k];
     if (tap != NO_TAP) {
 #pragma unroll
         for (int l = 0; l < V; l++) {

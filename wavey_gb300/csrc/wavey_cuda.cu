@@ -120,7 +120,8 @@ struct wavey_cuda_plan {
     std::vector<DevBuf> bufs;
     // device pointers
     void *field[2] = {nullptr, nullptr};
-    uint32_t *mask = nullptr, *sp_cell = nullptr, *sp_meta = nullptr, *sp_slot0 = nullptr, *sp_tap = nullptr, *recv = nullptr;
+    uint32_t *mask = nullptr, *recv = nullptr;
+    uint4 *sp = nullptr;
     void *slots = nullptr, *su = nullptr, *sg = nullptr, *tapw = nullptr, *sig = nullptr, *ring = nullptr, *tw = nullptr,
          *ir = nullptr;
     double *acc = nullptr, *freqs = nullptr;
@@ -243,10 +244,7 @@ void fill_args(wavey_cuda_plan *pl, wk::StepArgs<T> &a, int parity) {
     a.cur = reinterpret_cast<const T *>(pl->field[parity]);
     a.nxt = reinterpret_cast<T *>(pl->field[parity ^ 1]);
     a.interior = pl->mask;
-    a.sp_cell = pl->sp_cell;
-    a.sp_meta = pl->sp_meta;
-    a.sp_slot0 = pl->sp_slot0;
-    a.sp_tap = pl->sp_tap;
+    a.sp = pl->sp;
     a.slots = reinterpret_cast<const T *>(pl->slots);
     a.su = reinterpret_cast<T *>(pl->su);
     a.sg = reinterpret_cast<T *>(pl->sg);
@@ -377,10 +375,7 @@ void launch_step_half(wavey_cuda_plan *pl, int t, int parity) {
     a.cur = reinterpret_cast<const __half *>(pl->field[parity]);
     a.nxt = reinterpret_cast<__half *>(pl->field[parity ^ 1]);
     a.interior = pl->mask;
-    a.sp_cell = pl->sp_cell;
-    a.sp_meta = pl->sp_meta;
-    a.sp_slot0 = pl->sp_slot0;
-    a.sp_tap = pl->sp_tap;
+    a.sp = pl->sp;
     a.slots = reinterpret_cast<const float *>(pl->slots);
     a.su = reinterpret_cast<float *>(pl->su);
     a.sg = reinterpret_cast<float *>(pl->sg);
@@ -761,10 +756,11 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     for (int k = 0; k < 2; k++)
         if ((st = alloc(pl, &pl->field[k], pl->field_bytes))) return bail(st);
     if ((st = upload(pl, &pl->mask, mask.data(), mask.size() * 4))) return bail(st);
-    if ((st = upload(pl, &pl->sp_cell, cell_l.data(), cell_l.size() * 4))) return bail(st);
-    if ((st = upload(pl, &pl->sp_meta, meta_l.data(), meta_l.size() * 4))) return bail(st);
-    if ((st = upload(pl, &pl->sp_slot0, slot0_l.data(), slot0_l.size() * 4))) return bail(st);
-    if ((st = upload(pl, &pl->sp_tap, tap_l.data(), tap_l.size() * 4))) return bail(st);
+    {
+        std::vector<uint4> rec(cell_l.size());
+        for (size_t i = 0; i < rec.size(); i++) rec[i] = make_uint4(cell_l[i], meta_l[i], slot0_l[i], tap_l[i]);
+        if ((st = upload(pl, &pl->sp, rec.data(), rec.size() * sizeof(uint4)))) return bail(st);
+    }
     std::vector<double> slot_v(grid->slots ? grid->slots : (const double *)nullptr,
                                grid->slots ? grid->slots + 4 * nslots : (const double *)nullptr);
     std::vector<double> sig_v;
