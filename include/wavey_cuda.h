@@ -90,7 +90,9 @@ typedef struct {
     int64_t graph_kernels;                /* kernels per replay of the 128-step graph */
     int32_t interior_kernel;              /* 1: TMA-fed z-march beside the special-cell kernel; 0: fused step kernel */
     int32_t tma_zt;                       /* z planes per CTA of the TMA kernel */
-    int32_t tma_depth;                    /* ring depth of the TMA kernel (0: 6/4, 1: 8/6, 2: 11/9 planes) */
+    int32_t tma_depth;                    /* shape of the TMA kernel, rows/p ring/old ring: 0: 8/6/4, 1: 8/8/4,
+                                             2: 16/6/4, 3: 16/8/4, 4: 16/5/3 (-1: no TMA kernel) */
+    int32_t branch;                       /* form of the special-cell branch beside it (see wavey_tune_result) */
 } wavey_plan_info;
 
 int wavey_cuda_create(int device, wavey_cuda_ctx **out);
@@ -130,17 +132,22 @@ int wavey_cuda_plan_run(wavey_cuda_plan *plan, const volatile int32_t *cancel, v
 int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out);
 int wavey_cuda_plan_info(const wavey_cuda_plan *plan, wavey_plan_info *info);
 
-/* Autotuner of a plan's interior kernel (FP32 plans of at least 256 steps):
- * every candidate shape -- tile rows (8 or 16) with ring depths, and z
- * planes per CTA (8, 16, 32) -- runs two 128-step chunks of the plan's own
- * grid, and the plan keeps the fastest.  result (nullable) lists the
- * candidates' step times.  Other plans are left as they are. */
-#define WAVEY_TUNE_MAX 32
+/* Autotuner of a plan's step kernels (FP32 plans of at least 256 steps).
+ * Stage 1 times every shape of the interior kernel -- tile rows (8 or 16)
+ * with ring depths, and z planes per CTA (8, 16, 32 and the runs that fill
+ * one to four whole waves of resident CTAs); stage 2 times, with that shape,
+ * every form of the concurrent special-cell branch -- its register cap
+ * (branch / 3: 1, 3 or 4 blocks per SM) and launch priority (branch % 3:
+ * equal, special cells first, interior first).  Each candidate runs two
+ * 128-step chunks of the plan's own grid, and the plan keeps the fastest.
+ * result (nullable) lists the candidates' step times.  Neither stage changes
+ * any arithmetic.  Other plans are left as they are. */
+#define WAVEY_TUNE_MAX 64
 typedef struct {
-    int32_t cfg, zt, rows, p_planes, q_planes;
+    int32_t cfg, zt, rows, p_planes, q_planes, branch;
     double step_us;
     int32_t candidates;
-    int32_t cand_cfg[WAVEY_TUNE_MAX], cand_zt[WAVEY_TUNE_MAX];
+    int32_t cand_cfg[WAVEY_TUNE_MAX], cand_zt[WAVEY_TUNE_MAX], cand_branch[WAVEY_TUNE_MAX];
     double cand_step_us[WAVEY_TUNE_MAX];
 } wavey_tune_result;
 int wavey_cuda_plan_autotune(wavey_cuda_plan *plan, wavey_tune_result *result);

@@ -78,17 +78,18 @@ def test_per_source_signals(backend):
 
 
 def test_autotuned_plan_gives_identical_results(backend):
-    """The autotuner only changes the interior kernel's shape, never its
-    arithmetic: results before and after tuning are identical."""
+    """The autotuner only changes the interior kernel's shape and the launch
+    form of the special-cell branch, never the arithmetic: results before and
+    after tuning are identical."""
     g, taps, sig, rcv, freqs = spread_source()
     plan = backend.plan(g, [taps, taps], sig[:700], rcv, freqs, ir=True)
     plan.run()
     before = plan.read()
     res = plan.autotune()
     assert res["candidates"] and res["step_us"] > 0
-    assert res["step_us"] == min(c[2] for c in res["candidates"])
+    assert res["step_us"] == min(c[3] for c in res["candidates"])
     plan.run()
     after = plan.read()
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
-    assert plan.info()["tma_zt"] == res["zt"]
+    assert plan.info()["tma_zt"] == res["zt"] and plan.info()["branch"] == res["branch"]
     plan.close()

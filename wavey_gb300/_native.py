@@ -114,19 +114,19 @@ class WaveyPlanInfo(C.Structure):
         ("receivers", C.c_int64), ("freqs", C.c_int64), ("steps", C.c_int64),
         ("device_bytes", C.c_int64), ("padded_nx", C.c_int64), ("precision", C.c_int32),
         ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("graph_kernels", C.c_int64),
-        ("interior_kernel", C.c_int32), ("tma_zt", C.c_int32), ("tma_depth", C.c_int32),
+        ("interior_kernel", C.c_int32), ("tma_zt", C.c_int32), ("tma_depth", C.c_int32), ("branch", C.c_int32),
     ]
 
 
-WAVEY_TUNE_MAX = 32
+WAVEY_TUNE_MAX = 64
 
 
 class WaveyTuneResult(C.Structure):
     _fields_ = [
         ("cfg", C.c_int32), ("zt", C.c_int32), ("rows", C.c_int32), ("p_planes", C.c_int32), ("q_planes", C.c_int32),
-        ("step_us", C.c_double), ("candidates", C.c_int32),
+        ("branch", C.c_int32), ("step_us", C.c_double), ("candidates", C.c_int32),
         ("cand_cfg", C.c_int32 * WAVEY_TUNE_MAX), ("cand_zt", C.c_int32 * WAVEY_TUNE_MAX),
-        ("cand_step_us", C.c_double * WAVEY_TUNE_MAX),
+        ("cand_branch", C.c_int32 * WAVEY_TUNE_MAX), ("cand_step_us", C.c_double * WAVEY_TUNE_MAX),
     ]
 
 

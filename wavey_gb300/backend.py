@@ -314,14 +314,17 @@ class Plan:
         return (out, irbuf) if self.ir else out
 
     def autotune(self) -> dict:
-        """Times every candidate shape of the interior kernel on this plan's
-        grid and keeps the fastest (wavey_cuda_plan_autotune)."""
+        """Times every candidate shape of the interior kernel, then every
+        launch form of the special-cell branch, on this plan's grid and keeps
+        the fastest (wavey_cuda_plan_autotune).  Candidates are
+        (cfg, zt, branch, step_us)."""
         r = N.WaveyTuneResult()
         with self._b._lock:
             self._b._check(self._b._lib.wavey_cuda_plan_autotune(self._h, C.byref(r)))
         return {"cfg": r.cfg, "zt": r.zt, "rows": r.rows, "p_planes": r.p_planes, "q_planes": r.q_planes,
-                "step_us": r.step_us,
-                "candidates": [(r.cand_cfg[i], r.cand_zt[i], r.cand_step_us[i]) for i in range(r.candidates)]}
+                "branch": r.branch, "step_us": r.step_us,
+                "candidates": [(r.cand_cfg[i], r.cand_zt[i], r.cand_branch[i], r.cand_step_us[i])
+                               for i in range(r.candidates)]}
 
     def info(self) -> dict:
         i = N.WaveyPlanInfo()

@@ -179,7 +179,7 @@ __device__ __forceinline__ void load_slot(const StepArgs<T> &a, const T *SU, con
     r.g = load<T, V, false>(SG + j * V);
 }
 
-template <class T, int V, bool RUST_ORDER>
+template <class T, int V, bool RUST_ORDER, int SR = SLOT_REGS>
 __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, long long n) {
     const long long nxy = (long long)a.nxp * a.ny;
     const int c = (int)(k / a.n_special);
@@ -202,9 +202,9 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
 #pragma unroll
     for (int d = 0; d < 6; d++)
         if ((m >> d) & 1u) nb[d] = load<T, V, true>(P + (cell + offs[d]) * V);
-    SlotRegs<T, V> sr[SLOT_REGS];
+    SlotRegs<T, V> sr[SR > 0 ? SR : 1];
 #pragma unroll
-    for (int q = 0; q < SLOT_REGS; q++)
+    for (int q = 0; q < SR; q++)
         if (q < ns) load_slot<T, V>(a, SU, SG, j0 + q, sr[q]);
     // The laplacian over air neighbours in the -x,+x,-y,+y,-z,+z order.
     Lanes<T, V> sum;
@@ -233,9 +233,9 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
         for (int l = 0; l < V; l++) s2.v[l] = T(0);
         for (int q = 0; q < ns; q++) {
             SlotRegs<T, V> r;
-            if (q < SLOT_REGS) {
+            if (q < SR) {
 #pragma unroll
-                for (int i = 0; i < SLOT_REGS; i++)
+                for (int i = 0; i < SR; i++)
                     if (i == q) r = sr[i];
             } else {
                 load_slot<T, V>(a, SU, SG, j0 + q, r);
@@ -254,9 +254,9 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
             next.v[l] = rdiv(rsub(radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]), rmul(a.lam, s2.v[l])), den);
         for (int q = 0; q < ns; q++) {
             SlotRegs<T, V> r;
-            if (q < SLOT_REGS) {
+            if (q < SR) {
 #pragma unroll
-                for (int i = 0; i < SLOT_REGS; i++)
+                for (int i = 0; i < SR; i++)
                     if (i == q) r = sr[i];
             } else {
                 load_slot<T, V>(a, SU, SG, j0 + q, r);
@@ -367,6 +367,26 @@ __device__ __forceinline__ void step_block(const StepArgs<T> &a, int b, int t) {
 template <class T, int V, bool RUST_ORDER>
 __global__ void __launch_bounds__(BLOCK) fdtd_step(StepArgs<T> a, int t) {
     step_block<T, V, RUST_ORDER>(a, blockIdx.x, t);
+}
+
+// The special and record roles alone (interior_blocks == 0), for the branch
+// that runs beside the TMA interior kernel.  MINB caps the registers so that
+// MINB blocks fit an SM: a lighter branch leaves room for interior CTAs on
+// the same SMs.
+template <int V, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) special_branch(StepArgs<float> a, int t) {
+    constexpr int SR = MINB >= 4 ? (V == 4 ? 0 : 1) : MINB == 3 ? 2 : SLOT_REGS;  // slots held in registers
+    int b = blockIdx.x;
+    if (b < a.special_blocks) {
+        const long long k = (long long)b * BLOCK + threadIdx.x;
+        if (k >= (long long)a.n_special * a.chunks) return;
+        special_cell<float, V, false, SR>(a, k, *a.base + t);
+        return;
+    }
+    b -= a.special_blocks;
+    const long long k = (long long)b * BLOCK + threadIdx.x;
+    if (k >= (long long)a.n_recv * a.chunks) return;
+    record_one<float, V>(a, k, t);
 }
 
 // ----------------------------------------------------------- many rooms

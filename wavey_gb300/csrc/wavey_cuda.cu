@@ -144,7 +144,8 @@ struct wavey_cuda_plan {
     CUtensorMap tm_p[2], tm_q[2];  // per parity: p^n of field[parity], old of field[parity^1]
     int tma_tiles_x = 0, tma_tiles_y = 0, tma_tiles_z = 0, tma_zt = 32, tma_blocks = 0;
     int tma_cfg = 0;      // shape of the TMA kernel, an index into TMA_CFGS
-    int special_prio = 0;       // launch priority of the special-cell branch
+    int branch = 0;             // special-cell branch form: register cap (branch / 3) and priority (branch % 3)
+    int prio_lo = 0, prio_hi = 0;
     int *err = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_a = nullptr, ev_b = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
@@ -292,18 +293,29 @@ constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4}, {8, 8, 4}, {16, 6, 4}, {16, 8, 4}, {16
 constexpr int TMA_NCFG = 5;
 
 template <int V, int R, int NP, int NQ>
-void launch_tma(int blocks, cudaStream_t s, const CUtensorMap &p, const CUtensorMap &q, const wk::TmaArgs &ta) {
-    wk::interior_tma<V, R, NP, NQ><<<blocks, 256, wk::tma_smem_of<R, NP, NQ>(), s>>>(p, q, ta);
+void launch_tma(int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q, const wk::TmaArgs &ta) {
+    cudaLaunchConfig_t lc = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = prio;
+    lc.gridDim = dim3(blocks);
+    lc.blockDim = dim3(256);
+    lc.dynamicSmemBytes = wk::tma_smem_of<R, NP, NQ>();
+    lc.stream = s;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    cudaLaunchKernelEx(&lc, wk::interior_tma<V, R, NP, NQ>, p, q, ta);
 }
 
 template <int V>
-void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, const CUtensorMap &p, const CUtensorMap &q, const wk::TmaArgs &ta) {
+void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
+                    const wk::TmaArgs &ta) {
     switch (cfg) {
-        case 1: launch_tma<V, 8, 8, 4>(blocks, s, p, q, ta); break;
-        case 2: launch_tma<V, 16, 6, 4>(blocks, s, p, q, ta); break;
-        case 3: launch_tma<V, 16, 8, 4>(blocks, s, p, q, ta); break;
-        case 4: launch_tma<V, 16, 5, 3>(blocks, s, p, q, ta); break;
-        default: launch_tma<V, 8, 6, 4>(blocks, s, p, q, ta); break;
+        case 1: launch_tma<V, 8, 8, 4>(blocks, s, prio, p, q, ta); break;
+        case 2: launch_tma<V, 16, 6, 4>(blocks, s, prio, p, q, ta); break;
+        case 3: launch_tma<V, 16, 8, 4>(blocks, s, prio, p, q, ta); break;
+        case 4: launch_tma<V, 16, 5, 3>(blocks, s, prio, p, q, ta); break;
+        default: launch_tma<V, 8, 6, 4>(blocks, s, prio, p, q, ta); break;
     }
 }
 
@@ -338,13 +350,17 @@ void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
         cudaLaunchConfig_t lc = {};
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributePriority;
-        attr[0].val.priority = pl->special_prio;
+        attr[0].val.priority = pl->branch % 3 == 1 ? pl->prio_hi : pl->prio_lo;
         lc.blockDim = dim3(wk::BLOCK);
         lc.stream = side;
         lc.attrs = attr;
         lc.numAttrs = 1;
         lc.gridDim = dim3(pl->special_blocks + pl->record_blocks);
-        cudaLaunchKernelEx(&lc, wk::fdtd_step<float, V, false>, a, t);
+        switch (pl->branch / 3) {
+            case 1: cudaLaunchKernelEx(&lc, wk::special_branch<V, 3>, a, t); break;
+            case 2: cudaLaunchKernelEx(&lc, wk::special_branch<V, 4>, a, t); break;
+            default: cudaLaunchKernelEx(&lc, wk::special_branch<V, 1>, a, t); break;
+        }
     }
     if (pl->tma_blocks > 0) {
         wk::TmaArgs ta;
@@ -361,7 +377,8 @@ void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
         ta.tiles_z = pl->tma_tiles_z;
         ta.zt = pl->tma_zt;
         ta.l2 = (float)(COURANT * COURANT);
-        launch_tma_cfg<V>(pl->tma_cfg, pl->tma_blocks, s, pl->tm_p[parity], pl->tm_q[parity], ta);
+        launch_tma_cfg<V>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
+                          pl->tm_p[parity], pl->tm_q[parity], ta);
     }
     if (branch) {
         cudaEventRecord(pl->ev_join, side);
@@ -566,6 +583,52 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
     if (tb >= (1ll << 31)) return ctx->fail(WAVEY_E_LIMIT, "launch grid too large");
     pl->tma_blocks = (int)tb;
     return WAVEY_OK;
+}
+
+// Resident CTAs per SM of one shape of the TMA interior kernel.
+template <int V>
+int tma_occupancy(int cfg) {
+    int occ = 0;
+    const void *f;
+    size_t smem;
+    switch (cfg) {
+        case 1: f = (const void *)wk::interior_tma<V, 8, 8, 4>, smem = wk::tma_smem_of<8, 8, 4>(); break;
+        case 2: f = (const void *)wk::interior_tma<V, 16, 6, 4>, smem = wk::tma_smem_of<16, 6, 4>(); break;
+        case 3: f = (const void *)wk::interior_tma<V, 16, 8, 4>, smem = wk::tma_smem_of<16, 8, 4>(); break;
+        case 4: f = (const void *)wk::interior_tma<V, 16, 5, 3>, smem = wk::tma_smem_of<16, 5, 3>(); break;
+        default: f = (const void *)wk::interior_tma<V, 8, 6, 4>, smem = wk::tma_smem_of<8, 6, 4>(); break;
+    }
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, 256, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return occ;
+}
+
+// The z-run that makes the grid of one shape just fill w waves of resident
+// CTAs (every CTA of a launch does about the same work, so a partly filled
+// last wave idles SMs); 0 if none lies in 4..64 planes.
+int wave_zt(const wavey_cuda_plan *pl, int cfg, int w) {
+    const int occ = pl->V == 4 ? tma_occupancy<4>(cfg) : pl->V == 2 ? tma_occupancy<2>(cfg) : tma_occupancy<1>(cfg);
+    const int64_t planes = pl->nz - 2, rows = TMA_CFGS[cfg].rows, cells_row = wk::TMA_ROW_FLOATS / pl->V;
+    const int64_t layer = ((pl->nx + cells_row - 1) / cells_row) * ((pl->ny - 2 + rows - 1) / rows) * pl->chunks;
+    const int64_t slots = (int64_t)occ * pl->ctx->sm_count;
+    if (slots <= 0 || layer <= 0) return 0;
+    const int64_t runs = w * slots / layer;  // z-runs per column that fit w waves
+    if (runs < 1) return 0;
+    const int zt = (int)((planes + runs - 1) / runs);
+    return zt >= 4 && zt <= 64 ? zt : 0;
+}
+
+// Candidate z-runs of one shape: 8, 16 and 32 planes, and the runs that
+// fill one to four whole waves.
+std::vector<int> tune_zts(const wavey_cuda_plan *pl, int cfg) {
+    std::vector<int> zts = {8, 16, 32};
+    for (int w = 1; w <= 4; w++) {
+        const int zt = wave_zt(pl, cfg, w);
+        if (zt && std::find(zts.begin(), zts.end(), zt) == zts.end()) zts.push_back(zt);
+    }
+    return zts;
 }
 
 // standalone: a plan that runs by itself (TMA interior path where it
@@ -822,15 +885,19 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if ((st = ctx->cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event create"))) return bail(st);
     if ((st = alloc(pl, &pl->err, sizeof(int)))) return bail(st);
     if (standalone && precision == WAVEY_FP32 && tma_selected()) {
-        if ((st = tma_shape(pl, env_int("WAVEY_TMA_CFG", 0, 0, TMA_NCFG - 1), env_int("WAVEY_TMA_ZT", 16, 1, 4096))))
-            return bail(st);
+        // Untuned default: 16-row tiles with 5/3-plane rings, the z-run that
+        // fills one wave of resident CTAs, and a special-cell branch capped at
+        // three blocks per SM -- the shape the autotuner most often picks.
         cudaError_t e = tma_attrs<1>();
         if (e == cudaSuccess) e = tma_attrs<2>();
         if (e == cudaSuccess) e = tma_attrs<4>();
-        int lo_prio = 0, hi_prio = 0;
-        cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
-        pl->special_prio = env_int("WAVEY_SPECIAL_PRIO", 0, 0, 1) ? hi_prio : lo_prio;
         if ((st = ctx->cuda(e, "shared memory attribute"))) return bail(st);
+        const int cfg = env_int("WAVEY_TMA_CFG", 4, 0, TMA_NCFG - 1);
+        const int zw = wave_zt(pl, cfg, 1);
+        const int zt1 = zw ? std::max(8, zw) : 16;
+        if ((st = tma_shape(pl, cfg, env_int("WAVEY_TMA_ZT", zt1, 1, 4096)))) return bail(st);
+        cudaDeviceGetStreamPriorityRange(&pl->prio_lo, &pl->prio_hi);
+        pl->branch = env_int("WAVEY_BRANCH", 3, 0, 8);
         pl->tma = true;
     }
     if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
@@ -1124,43 +1191,54 @@ int rooms_run(wavey_cuda_rooms *rm, const volatile int32_t *cancel, void (*progr
 }
 
 
-// The autotuner: every candidate shape of the TMA interior kernel runs two
-// 128-step chunks of this plan's own grid; the fastest step span wins and
-// the plan keeps it.  Needs a TMA plan with at least 256 steps.
+// The autotuner.  Stage 1: every candidate shape of the TMA interior kernel
+// runs two 128-step chunks of this plan's own grid; the fastest step span
+// wins.  Stage 2: with that shape, every form of the special-cell branch.
+// The plan keeps the winner.  Needs a TMA plan with at least 256 steps.
 int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
     wavey_cuda_ctx *ctx = pl->ctx;
     if (res) *res = wavey_tune_result{};
     if (!pl->tma || pl->steps < 2 * wk::RING || !pl->graph) return WAVEY_OK;
-    static const int ZTS[] = {8, 16, 32};
-    int best_cfg = pl->tma_cfg, best_zt = pl->tma_zt, n = 0, st;
+    int best_cfg = pl->tma_cfg, best_zt = pl->tma_zt, best_branch = pl->branch, n = 0, st;
     double best = 1e30;
     cudaStream_t s = ctx->stream;
-    for (int cfg = 0; cfg < TMA_NCFG; cfg++)
-        for (int zt : ZTS) {
-            if ((st = tma_shape(pl, cfg, zt))) return st;
-            cudaGraphExecDestroy(pl->graph);
-            pl->graph = nullptr;
-            if ((st = build_graph(pl))) return st;
-            if ((st = plan_reset(pl))) return st;
-            float ms = 0.f;
-            for (int rep = 0; rep < 2; rep++) {
-                if ((st = ctx->cuda(cudaGraphLaunch(pl->graph, s), "graph launch"))) return st;
-                if ((st = ctx->cuda(cudaEventSynchronize(pl->ev_b), "tune wait"))) return st;
-                cudaEventElapsedTime(&ms, pl->ev_a, pl->ev_b);  // the second chunk's span counts
-            }
-            const double us = 1e3 * ms / wk::RING;
-            if (res && n < WAVEY_TUNE_MAX) {
-                res->cand_cfg[n] = cfg;
-                res->cand_zt[n] = zt;
-                res->cand_step_us[n] = us;
-            }
-            n++;
-            if (us < best) {
-                best = us;
-                best_cfg = cfg;
-                best_zt = zt;
-            }
+    auto trial = [&](int cfg, int zt, int branch) -> int {
+        pl->branch = branch;
+        if ((st = tma_shape(pl, cfg, zt))) return st;
+        cudaGraphExecDestroy(pl->graph);
+        pl->graph = nullptr;
+        if ((st = build_graph(pl))) return st;
+        if ((st = plan_reset(pl))) return st;
+        float ms = 0.f;
+        for (int rep = 0; rep < 2; rep++) {
+            if ((st = ctx->cuda(cudaGraphLaunch(pl->graph, s), "graph launch"))) return st;
+            if ((st = ctx->cuda(cudaEventSynchronize(pl->ev_b), "tune wait"))) return st;
+            cudaEventElapsedTime(&ms, pl->ev_a, pl->ev_b);  // the second chunk's span counts
         }
+        const double us = 1e3 * ms / wk::RING;
+        if (res && n < WAVEY_TUNE_MAX) {
+            res->cand_cfg[n] = cfg;
+            res->cand_zt[n] = zt;
+            res->cand_branch[n] = branch;
+            res->cand_step_us[n] = us;
+        }
+        n++;
+        if (us < best) {
+            best = us;
+            best_cfg = cfg;
+            best_zt = zt;
+            best_branch = branch;
+        }
+        return WAVEY_OK;
+    };
+    const int branch0 = pl->branch;
+    for (int cfg = 0; cfg < TMA_NCFG; cfg++)
+        for (int zt : tune_zts(pl, cfg))
+            if ((st = trial(cfg, zt, branch0))) return st;
+    const int cfg1 = best_cfg, zt1 = best_zt;
+    for (int branch = 0; branch < 9; branch++)
+        if (branch != branch0 && (st = trial(cfg1, zt1, branch))) return st;
+    pl->branch = best_branch;
     if ((st = tma_shape(pl, best_cfg, best_zt))) return st;
     cudaGraphExecDestroy(pl->graph);
     pl->graph = nullptr;
@@ -1169,6 +1247,7 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
     if (res) {
         res->cfg = best_cfg;
         res->zt = best_zt;
+        res->branch = best_branch;
         res->rows = TMA_CFGS[best_cfg].rows;
         res->p_planes = TMA_CFGS[best_cfg].np;
         res->q_planes = TMA_CFGS[best_cfg].nq;
@@ -1281,6 +1360,7 @@ int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
     info->interior_kernel = pl->tma ? 1 : 0;
     info->tma_zt = pl->tma ? pl->tma_zt : 0;
     info->tma_depth = pl->tma ? pl->tma_cfg : -1;
+    info->branch = pl->tma ? pl->branch : -1;
     return WAVEY_OK;
 }
 
