@@ -148,9 +148,9 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str):
+def profiled_traffic(workload: str, precision: str = "fp32"):
     """DRAM bytes per launch of the step kernel from the committed ncu summary."""
-    f = ROOT / "profiles" / f"fdtd_step_{workload}.md"
+    f = ROOT / "profiles" / (f"fdtd_step_{workload}.md" if precision == "fp32" else f"fdtd_step_{workload}_{precision}.md")
     if not f.exists():
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read_text())
@@ -250,7 +250,13 @@ def run_ours(args, rank, world):
     name, sms = b.device_info()
     log(f"[rank {rank}] {name} ({sms} SMs): {scene.name} grid {g.n}, air {g.air}, {scene.steps} steps, S={S}, "
         f"{len(scene.receivers)} receivers x {len(scene.freqs)} bins")
-    plan = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
+    from wavey_gb300.backend import FP16_STORAGE
+
+    main_precision = FP16_STORAGE if args.precision == "fp16" else FP32
+    bytes_per_update = 6 if args.precision == "fp16" else BYTES_PER_UPDATE
+    if args.precision == "fp16":
+        args.no_fp16 = True  # the main leg is the FP16 one
+    plan = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, main_precision)
     tuned = plan.autotune() if not args.no_autotune else None
     if tuned:
         log(f"[rank {rank}] autotuned: rows {tuned['rows']}, rings {tuned['p_planes']}/{tuned['q_planes']}, "
@@ -284,16 +290,16 @@ def run_ours(args, rank, world):
     # Roofline of the fused step kernel.
     peak, peak_kind = peaks()
     launch_s = step_ms / 1e3 / launches
-    alg_bytes = BYTES_PER_UPDATE * g.air * S
+    alg_bytes = bytes_per_update * g.air * S
     achieved = alg_bytes / launch_s / 1e9
-    traffic = profiled_traffic(args.workload)
+    traffic = profiled_traffic(args.workload, args.precision)
 
     # Plain: the same right-hand sides one at a time with the S = 1 kernel.
     plain = None
     if not args.no_plain:
         t_plain = 0.0
         for src in scene.sources:
-            p1 = b.plan(g, [src], scene.signal, scene.receivers, scene.freqs, FP32)
+            p1 = b.plan(g, [src], scene.signal, scene.receivers, scene.freqs, main_precision)
             p1.run()
             t_plain += p1.run(stats=True)["total_ms"] / 1e3
             p1.close()
@@ -304,7 +310,7 @@ def run_ours(args, rank, world):
     for _ in range(0 if getattr(args, "no_e2e_big", False) else args.e2e_steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        b.run_batch(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
+        b.run_batch(g, scene.sources, scene.signal, scene.receivers, scene.freqs, main_precision)
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = max_over_ranks(float(np.median(e2e_times)), world) if e2e_times else None
     e2e = updates_per_run * world / e2e_s / 1e9 if e2e_s else None
@@ -338,12 +344,18 @@ def run_ours(args, rank, world):
         from wavey_gb300.backend import FP16_STORAGE
 
         p16 = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP16_STORAGE)
+        tuned16 = p16.autotune() if not args.no_autotune else None
         p16.run()
         st16 = p16.run(stats=True)
+        info16 = p16.info()
         spec16 = p16.read()
         p16.close()
         fp16 = {"value": updates_per_run / (st16["total_ms"] / 1e3) / 1e9, "unit": UNIT,
-                "bytes_per_update": 6, "kernel": "fdtd_step_half (fused, register-queue z-march)"}
+                "bytes_per_update": 6,
+                "step_us": 1e3 * st16["step_ms"] / st16["step_launches"],
+                "kernel": ("interior_tma<__half> (TMA-fed z-march over FP16 planes) || fdtd_step_half special/record"
+                           if info16["interior_kernel"] else "fdtd_step_half (fused, register-queue z-march)"),
+                "autotuned": None if not tuned16 else {k: tuned16[k] for k in ("rows", "p_planes", "q_planes", "zt")}}
         if acc is not None:
             h0 = np.ones(len(scene.freqs), complex)
             t16 = np.stack([to_transfer(spec16[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
@@ -373,13 +385,16 @@ def run_ours(args, rank, world):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if args.precision == "fp32" else "f32 arithmetic, f16 field storage", "data": "synthetic",
             "config": {"workload": scene.name, "grid": list(g.n), "air_cells": g.air, "time_steps": scene.steps,
                        "right_hand_sides": S, "receivers": len(scene.receivers), "freq_bins": len(scene.freqs),
-                       "batched": True, "l2": "fields 2x%.0f MB > L2 (no flush needed)" % (info["device_bytes"] / 2e6),
+                       "batched": True,
+                       "l2": "fields 2x%.0f MB > L2 (no flush needed)" % (
+                           info["padded_nx"] * g.n[1] * g.n[2] * info["lanes"] * info["chunks"] * 4 / 1e6),
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU",
                        "autotuned": None if not tuned else {k: tuned[k] for k in ("rows", "p_planes", "q_planes", "zt",
-                                                                                  "step_us")}},
+                                                                                  "branch", "step_us")}},
             "per_source": value / S,
             "plain": {"value": plain, "per_source": None if plain is None else plain / S,
                       "batched_over_plain": None if plain is None else value / world / plain},
@@ -415,6 +430,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp16", action="store_true")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"],
+                    help="field storage of the main timed leg (fp16: FP16 storage, FP32 arithmetic)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--hall-steps", type=int, default=384)
     ap.add_argument("--hall-speakers", type=int, default=16)

@@ -167,15 +167,75 @@ __device__ __forceinline__ float store_h(__half *p, const Lanes<float, V> &v, fl
     return m;
 }
 
-// Raises the slab maximum, skipping the atomic when it cannot change it.
-__device__ __forceinline__ void raise_max(unsigned int *slot, float m) {
-    if (m > __uint_as_float(*reinterpret_cast<volatile unsigned int *>(slot))) atomicMax(slot, __float_as_uint(m));
-}
-
 __device__ __forceinline__ float warp_max(float m) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     return m;
+}
+
+// Field access of the special-cell update with FP16 storage: values are
+// scaled by their slab's power of two on load (level n for p, the planes
+// below and above for the z neighbours, level n-1 for p^(n-1)) and by the
+// inverse of level n+1's on store, which also raises the slab maximum.
+template <int V>
+struct HalfField {
+    const __half *P;
+    __half *Q;
+    float sm, sc, sp, so, inv;
+    int *error;
+    mutable float mx;  // max |p^(n+1)| stored, for the slab maximum
+    __device__ __forceinline__ Lanes<float, V> p(long long cell, int dz) const {
+        return load_h<V>(P + cell * V, dz < 0 ? sm : (dz > 0 ? sp : sc));
+    }
+    __device__ __forceinline__ Lanes<float, V> old(long long cell) const { return load_h<V>(Q + cell * V, so); }
+    __device__ __forceinline__ void put(long long cell, const Lanes<float, V> &v) const {
+        mx = store_h<V>(Q + cell * V, v, inv, error);
+    }
+};
+
+// Special cell k (over all chunks) at step n with FP16 storage.  Special
+// cells lie strictly inside the grid, so slabs z - 1 and z + 1 exist.
+template <int V, int SR>
+__device__ __forceinline__ void special_half(const HalfArgs &a, long long k, long long n, unsigned alive) {
+    const int c = (int)(k / a.n_special);
+    k -= (long long)c * a.n_special;
+    const uint4 rec = __ldg(a.sp + k);
+    const int z = (int)((long long)rec.x / ((long long)a.nxp * a.ny));
+    HalfField<V> f;
+    f.P = a.cur + (long long)c * a.cells_p * V;
+    f.Q = a.nxt + (long long)c * a.cells_p * V;
+    f.sm = slab_scale(a, n, c, z - 1).x;
+    f.sc = slab_scale(a, n, c, z).x;
+    f.sp = slab_scale(a, n, c, z + 1).x;
+    f.so = slab_scale(a, n + SCALE_RING - 1, c, z).x;
+    f.inv = slab_scale(a, n + 1, c, z).y;
+    f.error = a.error;
+    f.mx = 0.0f;
+    special_core<float, V, false, SR>(a, f, rec, c, n);
+    // Raise the slab maximum.  Special cells are sorted by cell, so a full
+    // warp mostly shares one slab and chunk: it combines first and issues one
+    // reduction without return (RED); otherwise every lane issues its own.
+    // alive: the lanes of this warp that hold a special cell.
+    unsigned int *slot = a.amax + ((long long)((n + 1) % AMAX_RING) * a.chunks + c) * a.nz + z;
+    __syncwarp(alive);
+    const int key = c * a.nz + z;
+    if (alive == 0xffffffffu && __all_sync(alive, key == __shfl_sync(alive, key, 0))) {
+        const float m = warp_max(f.mx);
+        if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(slot, __float_as_uint(m));
+    } else if (f.mx > 0.0f) {
+        atomicMax(slot, __float_as_uint(f.mx));
+    }
+}
+
+// Receiver k (over all chunks) into ring slot t: p^n in FP32.
+template <int V>
+__device__ __forceinline__ void record_half(const HalfArgs &a, long long k, int t, long long n) {
+    const int c = (int)(k / a.n_recv);
+    const long long r = k - (long long)c * a.n_recv;
+    const long long cell = a.recv[r];
+    const __half *P = a.cur + (long long)c * a.cells_p * V;
+    const Lanes<float, V> v = load_h<V>(P + cell * V, slab_scale(a, n, c, (int)(cell / ((long long)a.nxp * a.ny))).x);
+    store<float, V>(a.ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
 }
 
 template <int V>
@@ -223,7 +283,7 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step_half(HalfArgs a, int t) {
                 m = store_h<V>(Q + i * V, nx, s_new[z].y, a.error);
             }
             m = warp_max(m);
-            if (lane == 0 && m > 0.0f) raise_max(amax_new + c * a.nz + z, m);
+            if (lane == 0 && m > 0.0f) atomicMax(amax_new + c * a.nz + z, __float_as_uint(m));  // RED
             zm = zc;
             zc = zp;
             szm = szc;
@@ -233,106 +293,39 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step_half(HalfArgs a, int t) {
     }
     b -= a.interior_blocks;
     if (b < a.special_blocks) {
-        long long k = (long long)b * BLOCK + threadIdx.x;
-        if (k >= (long long)a.n_special * a.chunks) return;
-        const int c = (int)(k / a.n_special);
-        k -= (long long)c * a.n_special;
-        const uint4 rec = __ldg(a.sp + k);
-        const long long cell = rec.x;
-        const uint32_t m = rec.y;
-        const int z = (int)(cell / nxy);
-        const __half *P = a.cur + (long long)c * a.cells_p * V;
-        __half *Q = a.nxt + (long long)c * a.cells_p * V;
-        const float sc = slab_scale(a, n, c, z).x;
-        const Lanes<float, V> pc = load_h<V>(P + cell * V, sc);
-        const Lanes<float, V> pp = load_h<V>(Q + cell * V, slab_scale(a, n + SCALE_RING - 1, c, z).x);
-        const long long offs[6] = {-1, 1, -(long long)a.nxp, (long long)a.nxp, -nxy, nxy};
-        Lanes<float, V> sum;
-#pragma unroll
-        for (int l = 0; l < V; l++) sum.v[l] = 0.0f;
-        float kk = 0.0f;
-#pragma unroll
-        for (int d = 0; d < 6; d++) {
-            if ((m >> d) & 1u) {
-                const float sd = d < 4 ? sc : slab_scale(a, n, c, z + (d == 4 ? -1 : 1)).x;
-                const Lanes<float, V> nb = load_h<V>(P + (cell + offs[d]) * V, sd);
-#pragma unroll
-                for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb.v[l]);
-                kk = radd(kk, 1.0f);
-            }
-        }
-        Lanes<float, V> lap, next;
-#pragma unroll
-        for (int l = 0; l < V; l++) lap.v[l] = rmul(a.l2, rsub(sum.v[l], rmul(kk, pc.v[l])));
-        const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
-        if (ns == 0) {
-#pragma unroll
-            for (int l = 0; l < V; l++) next.v[l] = radd(rsub(rmul(2.0f, pc.v[l]), pp.v[l]), lap.v[l]);
-        } else {
-            const long long j0 = rec.z;
-            float *SU = a.su + (long long)c * a.n_slots * V;
-            float *SG = a.sg + (long long)c * a.n_slots * V;
-            float s1 = 0.0f;
-            Lanes<float, V> s2;
-#pragma unroll
-            for (int l = 0; l < V; l++) s2.v[l] = 0.0f;
-            for (int q = 0; q < ns; q++) {
-                const long long j = j0 + q;
-                const float4 sl = __ldg(reinterpret_cast<const float4 *>(a.slots) + j);
-                const Lanes<float, V> u = load<float, V, false>(SU + j * V);
-                const Lanes<float, V> g = load<float, V, false>(SG + j * V);
-#pragma unroll
-                for (int l = 0; l < V; l++) {
-                    const float e = rmul(radd(radd(rsub(rmul(sl.y, u.v[l]), rmul(sl.z, g.v[l])), rmul(0.5f, pc.v[l])),
-                                              rmul(sl.w, pp.v[l])),
-                                         sl.x);
-                    s2.v[l] = rsub(radd(s2.v[l], e), u.v[l]);
-                }
-                s1 = radd(s1, rmul(rsub(0.5f, sl.w), sl.x));
-            }
-            const float den = radd(1.0f, rmul(a.lam, s1));
-#pragma unroll
-            for (int l = 0; l < V; l++)
-                next.v[l] = rdiv(rsub(radd(rsub(rmul(2.0f, pc.v[l]), pp.v[l]), lap.v[l]), rmul(a.lam, s2.v[l])), den);
-            for (int q = 0; q < ns; q++) {
-                const long long j = j0 + q;
-                const float4 sl = __ldg(reinterpret_cast<const float4 *>(a.slots) + j);
-                Lanes<float, V> u = load<float, V, false>(SU + j * V);
-                Lanes<float, V> g = load<float, V, false>(SG + j * V);
-#pragma unroll
-                for (int l = 0; l < V; l++) {
-                    const float e = rmul(radd(radd(rsub(rmul(sl.y, u.v[l]), rmul(sl.z, g.v[l])), rmul(0.5f, pc.v[l])),
-                                              rmul(sl.w, pp.v[l])),
-                                         sl.x);
-                    const float un = radd(rmul(rmul(rsub(0.5f, sl.w), sl.x), next.v[l]), e);
-                    g.v[l] = radd(g.v[l], rmul(a.half_dt, radd(un, u.v[l])));
-                    u.v[l] = un;
-                }
-                store<float, V>(SU + j * V, u);
-                store<float, V>(SG + j * V, g);
-            }
-        }
-        const uint32_t tap = rec.w;
-        if (tap != NO_TAP) {
-#pragma unroll
-            for (int l = 0; l < V; l++) {
-                const int s = c * V + l;
-                next.v[l] = radd(next.v[l], rmul(a.sig[(long long)s * a.sig_stride + n], a.tapw[(long long)tap * a.lanes_total + s]));
-            }
-        }
-        const float mx = store_h<V>(Q + cell * V, next, slab_scale(a, n + 1, c, z).y, a.error);
-        if (mx > 0.0f) raise_max(amax_new + c * a.nz + z, mx);
+        const long long k = (long long)b * BLOCK + threadIdx.x;
+        const bool live = k < (long long)a.n_special * a.chunks;
+        const unsigned alive = __ballot_sync(0xffffffffu, live);
+        if (!live) return;
+        special_half<V, 0>(a, k, n, alive);  // lean: shares the kernel with the interior role
         return;
     }
     b -= a.special_blocks;
     const long long k = (long long)b * BLOCK + threadIdx.x;
     if (k >= (long long)a.n_recv * a.chunks) return;
-    const int c = (int)(k / a.n_recv);
-    const long long r = k - (long long)c * a.n_recv;
-    const long long cell = a.recv[r];
-    const __half *P = a.cur + (long long)c * a.cells_p * V;
-    const Lanes<float, V> v = load_h<V>(P + cell * V, slab_scale(a, n, c, (int)(cell / nxy)).x);
-    store<float, V>(a.ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
+    record_half<V>(a, k, t, n);
+}
+
+// The special and record roles alone (interior_blocks == 0), for the branch
+// beside the TMA interior kernel; MINB caps the registers as in
+// special_branch.
+template <int V, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) special_branch_half(HalfArgs a, int t) {
+    constexpr int SR = MINB >= 4 ? (V == 4 ? 0 : 1) : MINB == 3 ? 2 : SLOT_REGS;
+    const long long n = *a.base + t;
+    int b = blockIdx.x;
+    if (b < a.special_blocks) {
+        const long long k = (long long)b * BLOCK + threadIdx.x;
+        const bool live = k < (long long)a.n_special * a.chunks;
+        const unsigned alive = __ballot_sync(0xffffffffu, live);
+        if (!live) return;
+        special_half<V, SR>(a, k, n, alive);
+        return;
+    }
+    b -= a.special_blocks;
+    const long long k = (long long)b * BLOCK + threadIdx.x;
+    if (k >= (long long)a.n_recv * a.chunks) return;
+    record_half<V>(a, k, t, n);
 }
 
 }  // namespace wk

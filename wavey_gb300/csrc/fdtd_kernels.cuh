@@ -165,8 +165,8 @@ struct SlotRegs {
     Lanes<T, V> u, g;
 };
 
-template <class T, int V>
-__device__ __forceinline__ void load_slot(const StepArgs<T> &a, const T *SU, const T *SG, long long j, SlotRegs<T, V> &r) {
+template <class T, int V, class A>
+__device__ __forceinline__ void load_slot(const A &a, const T *SU, const T *SG, long long j, SlotRegs<T, V> &r) {
     if constexpr (sizeof(T) == 4) {
         const float4 c = __ldg(reinterpret_cast<const float4 *>(a.slots) + j);
         r.inv_d = c.x, r.cv = c.y, r.kb = c.z, r.w = c.w;
@@ -179,33 +179,43 @@ __device__ __forceinline__ void load_slot(const StepArgs<T> &a, const T *SU, con
     r.g = load<T, V, false>(SG + j * V);
 }
 
-template <class T, int V, bool RUST_ORDER, int SR = SLOT_REGS>
-__device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, long long n) {
+// Field access of the special-cell update for values stored as computed
+// (FP32, FP64): p^n at a cell (dz: its plane relative to the cell's, which
+// FP16 storage needs for the slab scale), p^(n-1), and the store of p^(n+1).
+template <class T, int V>
+struct PlainField {
+    const T *P;
+    T *Q;
+    __device__ __forceinline__ Lanes<T, V> p(long long cell, int) const { return load<T, V, true>(P + cell * V); }
+    __device__ __forceinline__ Lanes<T, V> old(long long cell) const { return load<T, V, false>(Q + cell * V); }
+    __device__ __forceinline__ void put(long long cell, const Lanes<T, V> &v) const { store<T, V>(Q + cell * V, v); }
+};
+
+// The special-cell update of chunk c at step n from its record rec, with
+// field access f (PlainField, or the FP16 form with slab scales) and the
+// step's arguments a (StepArgs or HalfArgs).
+template <class T, int V, bool RUST_ORDER, int SR, class A, class F>
+__device__ __forceinline__ void special_core(const A &a, const F &f, const uint4 rec, int c, long long n) {
     const long long nxy = (long long)a.nxp * a.ny;
-    const int c = (int)(k / a.n_special);
-    k -= (long long)c * a.n_special;
-    const uint4 rec = __ldg(a.sp + k);
     const long long cell = rec.x;
     const uint32_t m = rec.y;
     const long long j0 = rec.z;
     const uint32_t tap = rec.w;
-    const T *P = a.cur + (long long)c * a.cells_p * V;
-    T *Q = a.nxt + (long long)c * a.cells_p * V;
     const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
     T *SU = a.su + (long long)c * a.n_slots * V;
     T *SG = a.sg + (long long)c * a.n_slots * V;
     // All loads first.
-    const Lanes<T, V> pc = load<T, V, true>(P + cell * V);
-    const Lanes<T, V> pp = load<T, V, false>(Q + cell * V);
+    const Lanes<T, V> pc = f.p(cell, 0);
+    const Lanes<T, V> pp = f.old(cell);
     const long long offs[6] = {-1, 1, -(long long)a.nxp, (long long)a.nxp, -nxy, nxy};
     Lanes<T, V> nb[6];
 #pragma unroll
     for (int d = 0; d < 6; d++)
-        if ((m >> d) & 1u) nb[d] = load<T, V, true>(P + (cell + offs[d]) * V);
+        if ((m >> d) & 1u) nb[d] = f.p(cell + offs[d], d == 4 ? -1 : (d == 5 ? 1 : 0));
     SlotRegs<T, V> sr[SR > 0 ? SR : 1];
 #pragma unroll
     for (int q = 0; q < SR; q++)
-        if (q < ns) load_slot<T, V>(a, SU, SG, j0 + q, sr[q]);
+        if (q < ns) load_slot<T, V, A>(a, SU, SG, j0 + q, sr[q]);
     // The laplacian over air neighbours in the -x,+x,-y,+y,-z,+z order.
     Lanes<T, V> sum;
 #pragma unroll
@@ -222,7 +232,7 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
     Lanes<T, V> lap, next;
 #pragma unroll
     for (int l = 0; l < V; l++) lap.v[l] = rmul(a.l2, rsub(sum.v[l], rmul(kk, pc.v[l])));
-    const T half = T(0.5), two = T(2), one = T(1);
+    const T hf = T(0.5), two = T(2), one = T(1);
     if (ns == 0) {
 #pragma unroll
         for (int l = 0; l < V; l++) next.v[l] = radd(rsub(rmul(two, pc.v[l]), pp.v[l]), lap.v[l]);
@@ -238,15 +248,15 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
                 for (int i = 0; i < SR; i++)
                     if (i == q) r = sr[i];
             } else {
-                load_slot<T, V>(a, SU, SG, j0 + q, r);
+                load_slot<T, V, A>(a, SU, SG, j0 + q, r);
             }
 #pragma unroll
             for (int l = 0; l < V; l++) {
-                T e = rmul(radd(radd(rsub(rmul(r.cv, r.u.v[l]), rmul(r.kb, r.g.v[l])), rmul(half, pc.v[l])), rmul(r.w, pp.v[l])),
+                T e = rmul(radd(radd(rsub(rmul(r.cv, r.u.v[l]), rmul(r.kb, r.g.v[l])), rmul(hf, pc.v[l])), rmul(r.w, pp.v[l])),
                            r.inv_d);
                 s2.v[l] = RUST_ORDER ? radd(s2.v[l], rsub(e, r.u.v[l])) : rsub(radd(s2.v[l], e), r.u.v[l]);
             }
-            s1 = radd(s1, rmul(rsub(half, r.w), r.inv_d));
+            s1 = radd(s1, rmul(rsub(hf, r.w), r.inv_d));
         }
         const T den = radd(one, rmul(a.lam, s1));
 #pragma unroll
@@ -259,13 +269,13 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
                 for (int i = 0; i < SR; i++)
                     if (i == q) r = sr[i];
             } else {
-                load_slot<T, V>(a, SU, SG, j0 + q, r);
+                load_slot<T, V, A>(a, SU, SG, j0 + q, r);
             }
 #pragma unroll
             for (int l = 0; l < V; l++) {
-                T e = rmul(radd(radd(rsub(rmul(r.cv, r.u.v[l]), rmul(r.kb, r.g.v[l])), rmul(half, pc.v[l])), rmul(r.w, pp.v[l])),
+                T e = rmul(radd(radd(rsub(rmul(r.cv, r.u.v[l]), rmul(r.kb, r.g.v[l])), rmul(hf, pc.v[l])), rmul(r.w, pp.v[l])),
                            r.inv_d);
-                T un = radd(rmul(rmul(rsub(half, r.w), r.inv_d), next.v[l]), e);
+                T un = radd(rmul(rmul(rsub(hf, r.w), r.inv_d), next.v[l]), e);
                 r.g.v[l] = radd(r.g.v[l], rmul(a.half_dt, radd(un, r.u.v[l])));
                 r.u.v[l] = un;
             }
@@ -281,7 +291,16 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
             next.v[l] = radd(next.v[l], rmul(sv, a.tapw[(long long)tap * a.lanes_total + s]));
         }
     }
-    store<T, V>(Q + cell * V, next);
+    f.put(cell, next);
+}
+
+template <class T, int V, bool RUST_ORDER, int SR = SLOT_REGS>
+__device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, long long n) {
+    const int c = (int)(k / a.n_special);
+    k -= (long long)c * a.n_special;
+    const uint4 rec = __ldg(a.sp + k);
+    const PlainField<T, V> f{a.cur + (long long)c * a.cells_p * V, a.nxt + (long long)c * a.cells_p * V};
+    special_core<T, V, RUST_ORDER, SR>(a, f, rec, c, n);
 }
 
 // One receiver r of chunk c into ring slot t (the record role of fdtd_step).
@@ -354,7 +373,7 @@ __device__ __forceinline__ void step_block(const StepArgs<T> &a, int b, int t) {
         // ----------------------------------------------------- special
         const long long k = (long long)b * BLOCK + threadIdx.x;
         if (k >= (long long)a.n_special * a.chunks) return;
-        special_cell<T, V, RUST_ORDER>(a, k, *a.base + t);
+        special_cell<T, V, RUST_ORDER, 0>(a, k, *a.base + t);  // lean: shares the kernel with the interior role
         return;
     }
     b -= a.special_blocks;

@@ -21,6 +21,14 @@
 // The arithmetic is interior_update's (rounded separately, shader order), so
 // results are identical to the register-queue kernel's.
 //
+// The same kernel serves FP16 storage (E = __half): the rings then hold FP16
+// planes (a row is still 128 elements, the x halo 8 elements = 16 bytes so
+// every box starts on a 16-byte boundary), values are scaled by their slab's
+// power of two as they leave shared memory, p^(n+1) is stored with the next
+// level's scale, and every warp raises its slab maximum -- the operations of
+// fdtd_step_half's interior role in the same order, so the two give identical
+// results.
+//
 // Every wait on an mbarrier is bounded.  If one runs out, the kernel records
 // the failure in the error word, waits (again bounded) for the copies it has
 // issued, and returns; the host reports WAVEY_E_DEVICE.
@@ -28,13 +36,16 @@
 #include <cuda.h>
 #include <cstdint>
 
+#include "fdtd_half.cuh"
 #include "fdtd_kernels.cuh"
 
 namespace wk {
 
-constexpr int TMA_ROW_FLOATS = 128;         // floats per tile row (32 lanes x 16 B)
-constexpr int TMA_HALO_FLOATS = 4;          // 16-byte halo on each side in x
-constexpr int TMA_P_ROW = TMA_ROW_FLOATS + 2 * TMA_HALO_FLOATS;  // 136
+constexpr int TMA_ROW_FLOATS = 128;         // elements per tile row (32 lanes x 4)
+template <class E>
+__host__ __device__ constexpr int tma_halo() { return 16 / (int)sizeof(E); }  // 16-byte halo on each side in x
+template <class E>
+__host__ __device__ constexpr int tma_p_row() { return TMA_ROW_FLOATS + 2 * tma_halo<E>(); }  // 136 or 144
 
 constexpr uint32_t WAIT_LIMIT = 1u << 24;   // try_wait rounds before a wait is declared lost
 constexpr int ERR_TMA_WAIT = 1;
@@ -75,40 +86,70 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
+template <class E>
 struct TmaArgs {
     const uint32_t *interior;  // [nz][ny][nxw]
-    float *nxt;                // p^(n-1) in, p^(n+1) out, [chunks][cells_p][V]
+    E *nxt;                    // p^(n-1) in, p^(n+1) out, [chunks][cells_p][V]
     int *error;                // error word
     long long cells_p;
     int nxp, ny, nz, nxw;
     int tiles_x, tiles_y, tiles_z, zt;
     float l2;
+    // FP16 storage only: the step (*base + t), slab scales and maxima.
+    const long long *base;
+    int t, chunks;
+    const float2 *scale;       // [SCALE_RING][chunks][nz]
+    unsigned int *amax;        // [AMAX_RING][chunks][nz]
 };
+
+// Four consecutive elements of shared memory as floats (times the slab scale sc for FP16).
+__device__ __forceinline__ void ld4(const float *p, float o[4], float) {
+    const float4 v = *reinterpret_cast<const float4 *>(p);
+    o[0] = v.x, o[1] = v.y, o[2] = v.z, o[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const __half *p, float o[4], float sc) {
+    const uint2 raw = *reinterpret_cast<const uint2 *>(p);
+    const __half2 a = *reinterpret_cast<const __half2 *>(&raw.x), b = *reinterpret_cast<const __half2 *>(&raw.y);
+    o[0] = __low2float(a) * sc;
+    o[1] = __high2float(a) * sc;
+    o[2] = __low2float(b) * sc;
+    o[3] = __high2float(b) * sc;
+}
 
 // V: sources per cell in a chunk (1, 2 or 4); a tile row holds 128 / V cells.
 // R: rows per tile (8 or 16; 256 threads, R / 8 rows per thread).
 // NP / NQ: planes in the two rings; NP - 3 p planes and NQ - 1 old planes are
 // in flight while one plane is computed.
-template <int R>
-__host__ __device__ constexpr uint32_t tma_p_bytes() { return TMA_P_ROW * (R + 2) * 4; }
-template <int R>
-__host__ __device__ constexpr uint32_t tma_p_stride() { return (tma_p_bytes<R>() + 127) / 128 * 128; }
-template <int R>
-__host__ __device__ constexpr uint32_t tma_q_bytes() { return TMA_ROW_FLOATS * R * 4; }
-template <int R, int NP, int NQ>
-__host__ __device__ constexpr uint32_t tma_smem_of() { return NP * tma_p_stride<R>() + NQ * tma_q_bytes<R>() + 256 + 128; }
+template <class E, int R>
+__host__ __device__ constexpr uint32_t tma_p_bytes() { return tma_p_row<E>() * (R + 2) * sizeof(E); }
+template <class E, int R>
+__host__ __device__ constexpr uint32_t tma_p_stride() { return (tma_p_bytes<E, R>() + 127) / 128 * 128; }
+template <class E, int R>
+__host__ __device__ constexpr uint32_t tma_q_bytes() { return TMA_ROW_FLOATS * R * sizeof(E); }
+// FP16: the slab scales of a CTA's z-run, staged in shared memory (z-runs of
+// FP16 plans are at most TMA_MAX_ZT planes).
+constexpr int TMA_MAX_ZT = 64;
+constexpr int TMA_SCALE_STRIDE = TMA_MAX_ZT + 2;
+template <class E>
+__host__ __device__ constexpr uint32_t tma_scale_bytes() { return sizeof(E) == 2 ? 4 * TMA_SCALE_STRIDE * 4 : 0; }
+template <class E, int R, int NP, int NQ>
+__host__ __device__ constexpr uint32_t tma_smem_of() {
+    return NP * tma_p_stride<E, R>() + NQ * tma_q_bytes<E, R>() + 256 + tma_scale_bytes<E>() + 128;
+}
 
-template <int V, int R, int NP, int NQ>
+template <class E, int V, int R, int NP, int NQ>
 __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUtensorMap tm_p,
-                                                    const __grid_constant__ CUtensorMap tm_q, TmaArgs a) {
+                                                    const __grid_constant__ CUtensorMap tm_q, TmaArgs<E> a) {
+    constexpr bool HALF = sizeof(E) == 2;
     constexpr int RT = R / 8;                    // rows per thread
-    constexpr uint32_t PB = tma_p_bytes<R>(), PS = tma_p_stride<R>(), QB = tma_q_bytes<R>();
+    constexpr int HALO = tma_halo<E>(), PROW = tma_p_row<E>();
+    constexpr uint32_t PB = tma_p_bytes<E, R>(), PS = tma_p_stride<E, R>(), QB = tma_q_bytes<E, R>();
     constexpr int CELLS = TMA_ROW_FLOATS / V;    // cells per tile row
     constexpr uint32_t GROUP = (1u << (4 / V)) - 1u;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     unsigned char *base = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
-    float *Pbuf = reinterpret_cast<float *>(base);
-    float *Qbuf = reinterpret_cast<float *>(base + NP * PS);
+    E *Pbuf = reinterpret_cast<E *>(base);
+    E *Qbuf = reinterpret_cast<E *>(base + NP * PS);
     uint64_t *bars = reinterpret_cast<uint64_t *>(base + NP * PS + NQ * QB);
     const uint32_t barP = smem_addr(bars), barQ = smem_addr(bars + NP);
 
@@ -128,6 +169,26 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
     const int Kp = Kq + 2;       // p planes zs-1 .. ze
     const int cx = tx * TMA_ROW_FLOATS;
 
+    // FP16: slab scales of the z-run -- p^n of planes zs-1..ze (2^E of level
+    // n), p^(n-1) of planes zs..ze-1 (level n-1), the inverse scales of level
+    // n+1 for the stores and their range limits -- staged once, so no plane
+    // waits on them.
+    float *ssc = reinterpret_cast<float *>(base + NP * PS + NQ * QB + 256);
+    if constexpr (HALF) {
+        const long long n = *a.base + a.t;
+        const float2 *s_now = a.scale + ((int)(n % SCALE_RING) * a.chunks + c) * a.nz;
+        const float2 *s_old = a.scale + ((int)((n + SCALE_RING - 1) % SCALE_RING) * a.chunks + c) * a.nz;
+        const float2 *s_new = a.scale + ((int)((n + 1) % SCALE_RING) * a.chunks + c) * a.nz;
+        for (int i = threadIdx.x; i < Kp; i += 256) ssc[i] = s_now[zs - 1 + i].x;
+        for (int i = threadIdx.x; i < Kq; i += 256) {
+            ssc[TMA_SCALE_STRIDE + i] = s_old[zs + i].x;
+            ssc[2 * TMA_SCALE_STRIDE + i] = s_new[zs + i].y;
+            // Largest |p^(n+1)| the plane can store: 65504 * 2^E, as float bits
+            // (at most FLT_MAX's, so that infinities and NaNs exceed it).
+            ssc[3 * TMA_SCALE_STRIDE + i] =
+                __uint_as_float(min(__float_as_uint(65504.0f * s_new[zs + i].x), 0x7f7fffffu));
+        }
+    }
     if (threadIdx.x == 0) {
         for (int i = 0; i < NP + NQ; i++) mbar_init(smem_addr(bars + i), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -140,7 +201,7 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
         const int k = np_issued++;
         const uint32_t bar = barP + 8 * (k % NP);
         mbar_expect_tx(bar, PB);
-        tma_load_4d(smem_addr(Pbuf) + (k % NP) * PS, &tm_p, cx - TMA_HALO_FLOATS, y0 - 1, zs - 1 + k, c, bar);
+        tma_load_4d(smem_addr(Pbuf) + (k % NP) * PS, &tm_p, cx - HALO, y0 - 1, zs - 1 + k, c, bar);
     };
     auto issue_q = [&]() {
         const int j = nq_issued++;
@@ -154,9 +215,18 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
     }
 
     const int x0 = tx * CELLS + lane * (4 / V);
-    float *Q = a.nxt + (long long)c * a.cells_p * V;
+    E *Q = a.nxt + (long long)c * a.cells_p * V;
     const long long mstep = (long long)a.ny * a.nxw;
-    // Interior-mask words, four planes ahead, per row of this thread.
+    // FP16: the maxima slot of level n+1, and the scales of planes j and j+1.
+    unsigned int *amax_new = nullptr;
+    float scm = 1.0f, scc = 1.0f;
+    if constexpr (HALF) {
+        amax_new = a.amax + ((long long)((*a.base + a.t + 1) % AMAX_RING) * a.chunks + c) * a.nz;
+        scm = ssc[0];
+        scc = ssc[1];
+    }
+    // Rows of this thread: tile rows warp + 8 r (r < RT).  Interior-mask
+    // words, four planes ahead, per row.
     bool rok[RT];
     const uint32_t *mrow[RT];
     uint32_t mw[RT][4];
@@ -168,6 +238,7 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
 #pragma unroll
         for (int d = 0; d < 4; d++) mw[r][d] = (rok[r] && d < Kq) ? __ldg(mrow[r] + d * mstep) : 0u;
     }
+    const int g = HALO + lane * 4;  // this lane's four elements in a p row
     // Planes 0 and 1 of the p ring are waited for once; afterwards each plane
     // j waits only for p plane j + 2 and old plane j.
     bool ok = mbar_wait(barP, 0) && mbar_wait(barP + 8, 0);
@@ -181,13 +252,21 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
             if (np_issued < Kp) issue_p();
             if (nq_issued < Kq) issue_q();
         }
-        ok = ok && mbar_wait(barP + 8 * bp, php) && mbar_wait(barQ + 8 * bq, phq);
         const int z = zs + j;
+        float scp = 1.0f, sco = 1.0f, sinv = 1.0f, slim = 0.0f;
+        if constexpr (HALF) {
+            scp = ssc[j + 2];
+            sco = ssc[TMA_SCALE_STRIDE + j];
+            sinv = ssc[2 * TMA_SCALE_STRIDE + j];
+            slim = ssc[3 * TMA_SCALE_STRIDE + j];
+        }
+        ok = ok && mbar_wait(barP + 8 * bp, php) && mbar_wait(barQ + 8 * bq, phq);
+        uint32_t mb = 0;  // FP16: largest |p^(n+1)| stored, as float bits
         if (ok) {
-            const float *pm = Pbuf + bm * (PS / 4);
-            const float *pc = Pbuf + bc * (PS / 4);
-            const float *pn = Pbuf + bp * (PS / 4);
-            const float *qo = Qbuf + bq * (QB / 4);
+            const E *pc = Pbuf + bc * (PS / sizeof(E));
+            const E *pn = Pbuf + bp * (PS / sizeof(E));
+            const E *qo = Qbuf + bq * (QB / sizeof(E));
+            const E *pm = Pbuf + bm * (PS / sizeof(E));
 #pragma unroll
             for (int r = 0; r < RT; r++) {
                 const uint32_t word = mw[r][0];
@@ -198,20 +277,17 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
                 const uint32_t bits = (word >> (x0 & 31)) & GROUP;
                 if (!bits) continue;
                 const int row = warp + 8 * r;
-                const int g = TMA_HALO_FLOATS + lane * 4;
-                const float *rc = pc + (row + 1) * TMA_P_ROW;
-                const float4 cl = *reinterpret_cast<const float4 *>(rc + g - 4);
-                const float4 cc = *reinterpret_cast<const float4 *>(rc + g);
-                const float4 cr = *reinterpret_cast<const float4 *>(rc + g + 4);
-                const float4 ym = *reinterpret_cast<const float4 *>(pc + row * TMA_P_ROW + g);
-                const float4 yp = *reinterpret_cast<const float4 *>(pc + (row + 2) * TMA_P_ROW + g);
-                const float4 zm = *reinterpret_cast<const float4 *>(pm + (row + 1) * TMA_P_ROW + g);
-                const float4 zp = *reinterpret_cast<const float4 *>(pn + (row + 1) * TMA_P_ROW + g);
-                const float4 od = *reinterpret_cast<const float4 *>(qo + row * TMA_ROW_FLOATS + lane * 4);
-                const float w[12] = {cl.x, cl.y, cl.z, cl.w, cc.x, cc.y, cc.z, cc.w, cr.x, cr.y, cr.z, cr.w};
-                const float vym[4] = {ym.x, ym.y, ym.z, ym.w}, vyp[4] = {yp.x, yp.y, yp.z, yp.w};
-                const float vzm[4] = {zm.x, zm.y, zm.z, zm.w}, vzp[4] = {zp.x, zp.y, zp.z, zp.w};
-                const float vod[4] = {od.x, od.y, od.z, od.w};
+                const E *rc = pc + (row + 1) * PROW;
+                float w[12], vym[4], vyp[4], vod[4];
+                ld4(rc + g - 4, w, scc);
+                ld4(rc + g + 4, w + 8, scc);
+                ld4(rc + g, w + 4, scc);
+                float zmv[4], zpv[4];
+                ld4(pm + (row + 1) * PROW + g, zmv, scm);
+                ld4(pn + (row + 1) * PROW + g, zpv, scp);
+                ld4(pc + row * PROW + g, vym, scc);
+                ld4(pc + (row + 2) * PROW + g, vyp, scc);
+                ld4(qo + row * TMA_ROW_FLOATS + lane * 4, vod, sco);
                 float nx4[4];
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
@@ -219,12 +295,29 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
                     float s = radd(w[4 + e - V], w[4 + e + V]);
                     s = radd(s, vym[e]);
                     s = radd(s, vyp[e]);
-                    s = radd(s, vzm[e]);
-                    s = radd(s, vzp[e]);
+                    s = radd(s, zmv[e]);
+                    s = radd(s, zpv[e]);
                     nx4[e] = radd(rsub(rmul(2.0f, cv), vod[e]), rmul(a.l2, rsub(s, rmul(6.0f, cv))));
                 }
-                float *dst = Q + (((long long)z * a.ny + (y0 + row)) * a.nxp + x0) * V;
-                if (bits == GROUP) {
+                E *dst = Q + (((long long)z * a.ny + (y0 + row)) * a.nxp + x0) * V;
+                if constexpr (HALF) {
+                    const __half2 h01 = __floats2half2_rn(nx4[0] * sinv, nx4[1] * sinv);
+                    const __half2 h23 = __floats2half2_rn(nx4[2] * sinv, nx4[3] * sinv);
+#pragma unroll
+                    for (int e = 0; e < 4; e++)
+                        if ((bits >> (e / V)) & 1u) mb = max(mb, __float_as_uint(nx4[e]) & 0x7fffffffu);
+                    if (bits == GROUP) {
+                        uint2 raw;
+                        raw.x = *reinterpret_cast<const unsigned int *>(&h01);
+                        raw.y = *reinterpret_cast<const unsigned int *>(&h23);
+                        *reinterpret_cast<uint2 *>(dst) = raw;
+                    } else {
+                        const __half hv[4] = {__low2half(h01), __high2half(h01), __low2half(h23), __high2half(h23)};
+#pragma unroll
+                        for (int e = 0; e < 4; e++)
+                            if ((bits >> (e / V)) & 1u) dst[e] = hv[e];
+                    }
+                } else if (bits == GROUP) {
                     *reinterpret_cast<float4 *>(dst) = make_float4(nx4[0], nx4[1], nx4[2], nx4[3]);
                 } else {
 #pragma unroll
@@ -234,6 +327,17 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
                             for (int l = 0; l < V; l++) dst[q * V + l] = nx4[q * V + l];
                 }
             }
+        }
+        if constexpr (HALF) {
+            // A value beyond the FP16 range of its slab scale is an error,
+            // not a saturation; the warp's maximum raises the slab maximum by
+            // a reduction without return (RED).
+            if (mb > __float_as_uint(slim) && *reinterpret_cast<volatile int *>(a.error) == 0)
+                atomicExch(a.error, ERR_FP16_RANGE);
+            mb = __reduce_max_sync(0xffffffffu, mb);
+            if (lane == 0 && mb > 0u) atomicMax(amax_new + z, mb);
+            scm = scc;
+            scc = scp;
         }
         // One barrier per plane: everyone is done with this plane's buffers
         // (thread 0 refills them next), and a lost wait stops the whole CTA.

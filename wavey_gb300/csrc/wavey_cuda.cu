@@ -292,46 +292,72 @@ struct TmaCfg {
 constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4}, {8, 8, 4}, {16, 6, 4}, {16, 8, 4}, {16, 5, 3}};
 constexpr int TMA_NCFG = 5;
 
-template <int V, int R, int NP, int NQ>
-void launch_tma(int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q, const wk::TmaArgs &ta) {
+template <class E, int V, int R, int NP, int NQ>
+void launch_tma(int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
+                const wk::TmaArgs<E> &ta) {
     cudaLaunchConfig_t lc = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributePriority;
     attr[0].val.priority = prio;
     lc.gridDim = dim3(blocks);
     lc.blockDim = dim3(256);
-    lc.dynamicSmemBytes = wk::tma_smem_of<R, NP, NQ>();
+    lc.dynamicSmemBytes = wk::tma_smem_of<E, R, NP, NQ>();
     lc.stream = s;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    cudaLaunchKernelEx(&lc, wk::interior_tma<V, R, NP, NQ>, p, q, ta);
+    cudaLaunchKernelEx(&lc, wk::interior_tma<E, V, R, NP, NQ>, p, q, ta);
 }
 
-template <int V>
+template <class E, int V>
 void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
-                    const wk::TmaArgs &ta) {
+                    const wk::TmaArgs<E> &ta) {
     switch (cfg) {
-        case 1: launch_tma<V, 8, 8, 4>(blocks, s, prio, p, q, ta); break;
-        case 2: launch_tma<V, 16, 6, 4>(blocks, s, prio, p, q, ta); break;
-        case 3: launch_tma<V, 16, 8, 4>(blocks, s, prio, p, q, ta); break;
-        case 4: launch_tma<V, 16, 5, 3>(blocks, s, prio, p, q, ta); break;
-        default: launch_tma<V, 8, 6, 4>(blocks, s, prio, p, q, ta); break;
+        case 1: launch_tma<E, V, 8, 8, 4>(blocks, s, prio, p, q, ta); break;
+        case 2: launch_tma<E, V, 16, 6, 4>(blocks, s, prio, p, q, ta); break;
+        case 3: launch_tma<E, V, 16, 8, 4>(blocks, s, prio, p, q, ta); break;
+        case 4: launch_tma<E, V, 16, 5, 3>(blocks, s, prio, p, q, ta); break;
+        default: launch_tma<E, V, 8, 6, 4>(blocks, s, prio, p, q, ta); break;
     }
 }
 
-template <int V, int R, int NP, int NQ>
+template <class E, int V, int R, int NP, int NQ>
 cudaError_t tma_attr() {
-    return cudaFuncSetAttribute((const void *)wk::interior_tma<V, R, NP, NQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)wk::tma_smem_of<R, NP, NQ>());
+    return cudaFuncSetAttribute((const void *)wk::interior_tma<E, V, R, NP, NQ>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wk::tma_smem_of<E, R, NP, NQ>());
 }
 
-template <int V>
+template <class E, int V>
 cudaError_t tma_attrs() {
-    cudaError_t e[] = {tma_attr<V, 8, 6, 4>(), tma_attr<V, 8, 8, 4>(), tma_attr<V, 16, 6, 4>(), tma_attr<V, 16, 8, 4>(),
-                       tma_attr<V, 16, 5, 3>()};
+    cudaError_t e[] = {tma_attr<E, V, 8, 6, 4>(), tma_attr<E, V, 8, 8, 4>(), tma_attr<E, V, 16, 6, 4>(),
+                       tma_attr<E, V, 16, 8, 4>(), tma_attr<E, V, 16, 5, 3>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
+}
+
+// The TMA kernel's arguments for one step (FP16 fields are unused in FP32).
+template <class E>
+wk::TmaArgs<E> tma_args(const wavey_cuda_plan *pl, int t, int parity) {
+    wk::TmaArgs<E> ta;
+    ta.interior = pl->mask;
+    ta.nxt = reinterpret_cast<E *>(pl->field[parity ^ 1]);
+    ta.error = pl->err;
+    ta.cells_p = pl->cells_p;
+    ta.nxp = (int)pl->nxp;
+    ta.ny = (int)pl->ny;
+    ta.nz = (int)pl->nz;
+    ta.nxw = (int)(pl->nxp / 32);
+    ta.tiles_x = pl->tma_tiles_x;
+    ta.tiles_y = pl->tma_tiles_y;
+    ta.tiles_z = pl->tma_tiles_z;
+    ta.zt = pl->tma_zt;
+    ta.l2 = (float)(COURANT * COURANT);
+    ta.base = pl->base;
+    ta.t = t;
+    ta.chunks = pl->chunks;
+    ta.scale = pl->scale;
+    ta.amax = pl->amax;
+    return ta;
 }
 
 template <int V>
@@ -362,32 +388,16 @@ void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
             default: cudaLaunchKernelEx(&lc, wk::special_branch<V, 1>, a, t); break;
         }
     }
-    if (pl->tma_blocks > 0) {
-        wk::TmaArgs ta;
-        ta.interior = pl->mask;
-        ta.nxt = reinterpret_cast<float *>(pl->field[parity ^ 1]);
-        ta.error = pl->err;
-        ta.cells_p = pl->cells_p;
-        ta.nxp = (int)pl->nxp;
-        ta.ny = (int)pl->ny;
-        ta.nz = (int)pl->nz;
-        ta.nxw = (int)(pl->nxp / 32);
-        ta.tiles_x = pl->tma_tiles_x;
-        ta.tiles_y = pl->tma_tiles_y;
-        ta.tiles_z = pl->tma_tiles_z;
-        ta.zt = pl->tma_zt;
-        ta.l2 = (float)(COURANT * COURANT);
-        launch_tma_cfg<V>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
-                          pl->tm_p[parity], pl->tm_q[parity], ta);
-    }
+    if (pl->tma_blocks > 0)
+        launch_tma_cfg<float, V>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
+                                 pl->tm_p[parity], pl->tm_q[parity], tma_args<float>(pl, t, parity));
     if (branch) {
         cudaEventRecord(pl->ev_join, side);
         cudaStreamWaitEvent(s, pl->ev_join, 0);
     }
 }
 
-template <int V>
-void launch_step_half(wavey_cuda_plan *pl, int t, int parity) {
+wk::HalfArgs half_args(const wavey_cuda_plan *pl, int parity) {
     wk::HalfArgs a;
     a.cur = reinterpret_cast<const __half *>(pl->field[parity]);
     a.nxt = reinterpret_cast<__half *>(pl->field[parity ^ 1]);
@@ -427,13 +437,65 @@ void launch_step_half(wavey_cuda_plan *pl, int t, int parity) {
     a.lam = (float)COURANT;
     a.half_dt = 0.5f * (float)pl->dt;
     a.shift = pl->fp16_shift;
+    return a;
+}
+
+template <int V>
+void launch_step_half(wavey_cuda_plan *pl, int t, int parity) {
+    const wk::HalfArgs a = half_args(pl, parity);
     const int prep = (int)((pl->chunks * pl->nz + wk::BLOCK - 1) / wk::BLOCK);
     wk::half_prepare<V><<<prep, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
     const int blocks = pl->interior_blocks + pl->special_blocks + pl->record_blocks;
     if (blocks > 0) wk::fdtd_step_half<V><<<blocks, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
 }
 
+// FP16 storage with the TMA interior kernel: half_prepare fixes the scales of
+// level n+1, then the special-cell and receiver roles of fdtd_step_half run
+// beside the TMA kernel, as in the FP32 step.
+template <int V>
+void launch_step_half_tma(wavey_cuda_plan *pl, int t, int parity) {
+    cudaStream_t s = pl->ctx->stream, side = pl->ctx->side;
+    wk::HalfArgs a = half_args(pl, parity);
+    const int prep = (int)((pl->chunks * pl->nz + wk::BLOCK - 1) / wk::BLOCK);
+    wk::half_prepare<V><<<prep, wk::BLOCK, 0, s>>>(a, t);
+    a.interior_blocks = 0;
+    const int blocks = pl->special_blocks + pl->record_blocks;
+    if (blocks > 0) {
+        cudaEventRecord(pl->ev_fork, s);
+        cudaStreamWaitEvent(side, pl->ev_fork, 0);
+        cudaLaunchConfig_t lc = {};
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributePriority;
+        attr[0].val.priority = pl->branch % 3 == 1 ? pl->prio_hi : pl->prio_lo;
+        lc.blockDim = dim3(wk::BLOCK);
+        lc.gridDim = dim3(blocks);
+        lc.stream = side;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        switch (pl->branch / 3) {
+            case 1: cudaLaunchKernelEx(&lc, wk::special_branch_half<V, 3>, a, t); break;
+            case 2: cudaLaunchKernelEx(&lc, wk::special_branch_half<V, 4>, a, t); break;
+            default: cudaLaunchKernelEx(&lc, wk::special_branch_half<V, 1>, a, t); break;
+        }
+    }
+    if (pl->tma_blocks > 0)
+        launch_tma_cfg<__half, V>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
+                                  pl->tm_p[parity], pl->tm_q[parity], tma_args<__half>(pl, t, parity));
+    if (blocks > 0) {
+        cudaEventRecord(pl->ev_join, side);
+        cudaStreamWaitEvent(s, pl->ev_join, 0);
+    }
+}
+
 void step(wavey_cuda_plan *pl, int t, int parity) {
+    if (pl->tma && pl->precision == WAVEY_FP16_STORAGE) {
+        switch (pl->V) {
+            case 1: launch_step_half_tma<1>(pl, t, parity); break;
+            case 2: launch_step_half_tma<2>(pl, t, parity); break;
+            default: launch_step_half_tma<4>(pl, t, parity); break;
+        }
+        return;
+    }
     if (pl->tma) {
         switch (pl->V) {
             case 1: launch_step_tma<1>(pl, t, parity); break;
@@ -557,23 +619,26 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
     EncodeTiled enc = encode_tiled();
     if (!enc) return ctx->fail(WAVEY_E_CUDA, "the driver lacks cuTensorMapEncodeTiled");
     const int64_t V = pl->V, nx = pl->nx, ny = pl->ny, nz = pl->nz;
+    const bool half = pl->precision == WAVEY_FP16_STORAGE;
+    const int64_t es = half ? 2 : 4;
+    const CUtensorMapDataType dt = half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     const cuuint64_t dims[4] = {(cuuint64_t)(nx * V), (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)pl->chunks};
-    const cuuint64_t strides[3] = {(cuuint64_t)(pl->nxp * V * 4), (cuuint64_t)(pl->nxp * ny * V * 4),
-                                   (cuuint64_t)(pl->cells_p * V * 4)};
+    const cuuint64_t strides[3] = {(cuuint64_t)(pl->nxp * V * es), (cuuint64_t)(pl->nxp * ny * V * es),
+                                   (cuuint64_t)(pl->cells_p * V * es)};
     const int rows = TMA_CFGS[cfg].rows;
-    const cuuint32_t box_p[4] = {(cuuint32_t)wk::TMA_P_ROW, (cuuint32_t)(rows + 2), 1, 1};
+    const int prow = half ? wk::tma_p_row<__half>() : wk::tma_p_row<float>();
+    const cuuint32_t box_p[4] = {(cuuint32_t)prow, (cuuint32_t)(rows + 2), 1, 1};
     const cuuint32_t box_q[4] = {(cuuint32_t)wk::TMA_ROW_FLOATS, (cuuint32_t)rows, 1, 1};
     const cuuint32_t unit[4] = {1, 1, 1, 1};
     for (int k = 0; k < 2; k++) {
-        CUresult r1 = enc(&pl->tm_p[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k], dims, strides, box_p, unit,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        CUresult r2 = enc(&pl->tm_q[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, pl->field[k ^ 1], dims, strides, box_q, unit,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        CUresult r1 = enc(&pl->tm_p[k], dt, 4, pl->field[k], dims, strides, box_p, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        CUresult r2 = enc(&pl->tm_q[k], dt, 4, pl->field[k ^ 1], dims, strides, box_q, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS)
             return ctx->fail(WAVEY_E_CUDA, "tensor map encoding failed (%d, %d)", (int)r1, (int)r2);
     }
+    if (half) zt = std::min(zt, wk::TMA_MAX_ZT);  // the FP16 kernel stages a z-run's scales in shared memory
     pl->tma_cfg = cfg;
     pl->tma_zt = zt;
     pl->tma_tiles_x = (int)((nx + (wk::TMA_ROW_FLOATS / V) - 1) / (wk::TMA_ROW_FLOATS / V));
@@ -586,17 +651,17 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
 }
 
 // Resident CTAs per SM of one shape of the TMA interior kernel.
-template <int V>
+template <class E, int V>
 int tma_occupancy(int cfg) {
     int occ = 0;
     const void *f;
     size_t smem;
     switch (cfg) {
-        case 1: f = (const void *)wk::interior_tma<V, 8, 8, 4>, smem = wk::tma_smem_of<8, 8, 4>(); break;
-        case 2: f = (const void *)wk::interior_tma<V, 16, 6, 4>, smem = wk::tma_smem_of<16, 6, 4>(); break;
-        case 3: f = (const void *)wk::interior_tma<V, 16, 8, 4>, smem = wk::tma_smem_of<16, 8, 4>(); break;
-        case 4: f = (const void *)wk::interior_tma<V, 16, 5, 3>, smem = wk::tma_smem_of<16, 5, 3>(); break;
-        default: f = (const void *)wk::interior_tma<V, 8, 6, 4>, smem = wk::tma_smem_of<8, 6, 4>(); break;
+        case 1: f = (const void *)wk::interior_tma<E, V, 8, 8, 4>, smem = wk::tma_smem_of<E, 8, 8, 4>(); break;
+        case 2: f = (const void *)wk::interior_tma<E, V, 16, 6, 4>, smem = wk::tma_smem_of<E, 16, 6, 4>(); break;
+        case 3: f = (const void *)wk::interior_tma<E, V, 16, 8, 4>, smem = wk::tma_smem_of<E, 16, 8, 4>(); break;
+        case 4: f = (const void *)wk::interior_tma<E, V, 16, 5, 3>, smem = wk::tma_smem_of<E, 16, 5, 3>(); break;
+        default: f = (const void *)wk::interior_tma<E, V, 8, 6, 4>, smem = wk::tma_smem_of<E, 8, 6, 4>(); break;
     }
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, 256, smem) != cudaSuccess) {
         cudaGetLastError();
@@ -605,11 +670,17 @@ int tma_occupancy(int cfg) {
     return occ;
 }
 
+template <class E>
+int tma_occupancy_v(int V, int cfg) {
+    return V == 4 ? tma_occupancy<E, 4>(cfg) : V == 2 ? tma_occupancy<E, 2>(cfg) : tma_occupancy<E, 1>(cfg);
+}
+
 // The z-run that makes the grid of one shape just fill w waves of resident
 // CTAs (every CTA of a launch does about the same work, so a partly filled
 // last wave idles SMs); 0 if none lies in 4..64 planes.
 int wave_zt(const wavey_cuda_plan *pl, int cfg, int w) {
-    const int occ = pl->V == 4 ? tma_occupancy<4>(cfg) : pl->V == 2 ? tma_occupancy<2>(cfg) : tma_occupancy<1>(cfg);
+    const int occ = pl->precision == WAVEY_FP16_STORAGE ? tma_occupancy_v<__half>(pl->V, cfg)
+                                                         : tma_occupancy_v<float>(pl->V, cfg);
     const int64_t planes = pl->nz - 2, rows = TMA_CFGS[cfg].rows, cells_row = wk::TMA_ROW_FLOATS / pl->V;
     const int64_t layer = ((pl->nx + cells_row - 1) / cells_row) * ((pl->ny - 2 + rows - 1) / rows) * pl->chunks;
     const int64_t slots = (int64_t)occ * pl->ctx->sm_count;
@@ -884,13 +955,13 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     for (cudaEvent_t *e : {&pl->ev_fork, &pl->ev_join})
         if ((st = ctx->cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event create"))) return bail(st);
     if ((st = alloc(pl, &pl->err, sizeof(int)))) return bail(st);
-    if (standalone && precision == WAVEY_FP32 && tma_selected()) {
+    if (standalone && (precision == WAVEY_FP32 || precision == WAVEY_FP16_STORAGE) && tma_selected()) {
         // Untuned default: 16-row tiles with 5/3-plane rings, the z-run that
         // fills one wave of resident CTAs, and a special-cell branch capped at
         // three blocks per SM -- the shape the autotuner most often picks.
-        cudaError_t e = tma_attrs<1>();
-        if (e == cudaSuccess) e = tma_attrs<2>();
-        if (e == cudaSuccess) e = tma_attrs<4>();
+        cudaError_t e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 1>() : tma_attrs<float, 1>();
+        if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 2>() : tma_attrs<float, 2>();
+        if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 4>() : tma_attrs<float, 4>();
         if ((st = ctx->cuda(e, "shared memory attribute"))) return bail(st);
         const int cfg = env_int("WAVEY_TMA_CFG", 4, 0, TMA_NCFG - 1);
         const int zw = wave_zt(pl, cfg, 1);
