@@ -132,6 +132,29 @@ int wavey_cuda_plan_run(wavey_cuda_plan *plan, const volatile int32_t *cancel, v
 int wavey_cuda_plan_read(wavey_cuda_plan *plan, double *out, double *ir_out);
 int wavey_cuda_plan_info(const wavey_cuda_plan *plan, wavey_plan_info *info);
 
+/* Per-speaker transfer functions straight from a plan's device spectra, in
+ * the transfer section of results.bin (result.rs:444-456): complex64, mics
+ * first as [mic][speaker][f], then each plane as [speaker][point][f] -- the
+ * plan's receivers must be the mics followed by the planes' inside points
+ * in plane order (run.rs:380-392).  Speaker s's transfer is the sum over its
+ * right-hand sides of factor[lane][f] x spectrum[lane][r][f] (the factor
+ * carries the component weight, to_transfer's scale and the cabinet
+ * calibration, run.rs:631-660), summed in FP64 on the device; only the
+ * complex64 result crosses to the host.  Replaces reading every right-hand
+ * side's FP64 spectra and combining them on the host (Gpu::run_fdtd's
+ * Spectra, then to_transfer per component); no counterpart call in the
+ * reference. */
+typedef struct {
+    int32_t n_speakers;
+    const int32_t *lane_speaker;  /* [plan sources]: speaker of each right-hand side, -1 to leave it out */
+    const double *factor;         /* [plan sources][nf][2] complex factor per right-hand side and frequency */
+    int64_t n_mics;               /* receivers [0, n_mics) are mics */
+    int32_t n_planes;
+    const int64_t *plane_points;  /* [n_planes] inside points per plane, after the mics, in order */
+} wavey_transfer_layout;
+int wavey_cuda_plan_transfers(wavey_cuda_plan *plan, const wavey_transfer_layout *layout, float *out,
+                              size_t out_floats);
+
 /* Autotuner of a plan's step kernels (FP32 plans of at least 256 steps).
  * Stage 1 times every shape of the interior kernel -- tile rows (8 or 16)
  * with ring depths, and z planes per CTA (8, 16, 32 and the runs that fill

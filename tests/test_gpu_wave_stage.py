@@ -29,8 +29,8 @@ pytestmark = pytest.mark.gpu
 
 def test_wave_stage_matches_oracle_and_per_component_runs(backend):
     room, g, speakers, rx, freqs, steps, cab = small_solve(with_cabinet=True)
-    cal = calibrate_cabinets(backend, [cab], c, 354.0, 8.0, 4.0, freqs)
-    cal_o = calibrate_cabinets(OracleBackend(), [cab], c, 354.0, 8.0, 4.0, freqs)
+    cal = calibrate_cabinets(backend, [cab], c, 354.0, 8.0, 2.0, freqs)
+    cal_o = calibrate_cabinets(OracleBackend(), [cab], c, 354.0, 8.0, 2.0, freqs)
     assert worst_relative(cal_o[0].on_axis, cal[0].on_axis) < 2e-3
     assert worst_relative(cal_o[0].directivity, cal[0].directivity) < 2e-3
     cals = {"boxed": cal[0]}
@@ -87,3 +87,35 @@ def test_cardioid_speaker_reproduces_its_directivity(backend):
             fit = a0 + (a[0] * d[0] + a[1] * d[1] + a[2] * d[2]) / dist * (1.0 + 1.0 / (1j * k * dist))
             worst = max(worst, abs(card[ri, fi] / omni[ri, fi] - fit))
     assert worst < 0.05, worst
+
+
+def test_transfer_section_from_device_spectra(backend):
+    """wave_stage_results combines on the device and reads back complex64 in
+    the results.bin layout: equal to the host combination laid out the same
+    way, to complex64 rounding."""
+    from wavey_gb300.wave import layout_transfers, wave_stage_results
+
+    room, g, speakers, rx, freqs, steps, cab = small_solve(with_cabinet=True)
+    cals = {"boxed": calibrate_cabinets(backend, [cab], c, 354.0, 8.0, 2.0, freqs)[0]}
+    n_mics, planes = 1, [2, 1]  # receivers: one mic, then planes of two and one points
+    host = wave_stage(backend, g, speakers, rx, freqs, c, 354.0, steps, calibrations=cals)
+    want = layout_transfers(host.transfers, n_mics, planes)
+    got = wave_stage_results(backend, g, speakers, rx, n_mics, planes, freqs, c, 354.0, steps, calibrations=cals)
+    assert got.dtype == np.complex64 and got.shape == want.shape
+    assert np.abs(got - want).max() <= 1e-6 * np.abs(want).max()
+
+
+def test_transfer_layout_is_checked(backend):
+    from wavey_gb300.backend import WaveyError
+
+    room, g, speakers, rx, freqs, steps, _ = small_solve()
+    plan = backend.plan(g, [g.taps_at(speakers[0].position)], np.zeros(200), rx, freqs)
+    plan.run()
+    fac = np.ones((1, len(freqs)), complex)
+    with pytest.raises(WaveyError, match="receivers"):
+        plan.transfers([0], fac, 1, [1])  # 2 receivers laid out, the plan has 4
+    with pytest.raises(WaveyError, match="speaker"):
+        plan.transfers([-2], fac, 4)
+    out = plan.transfers([0], fac, 4)
+    assert out.shape == (4 * len(freqs),)
+    plan.close()

@@ -93,3 +93,50 @@ def test_calibrations_run_as_one_multi_room_call():
     ref = per_component_reference(OracleBackend(), g, speakers, rx, freqs, steps, 354.0,
                                   calibrations={"boxed": cal[0]})
     assert worst_relative(ref[2], res.transfers[2]) == 0.0
+
+
+def _save_layout_like_reference(transfers, n_mics, plane_points):
+    """result.rs:444-456 written out: every mic's transfer per speaker, then
+    every plane's transfer per speaker, each a run of Complex32."""
+    out = []
+    for m in range(n_mics):
+        for s in range(len(transfers)):
+            out.extend(np.asarray(transfers[s][m], dtype=np.complex64))
+    r0 = n_mics
+    for pts in plane_points:
+        for s in range(len(transfers)):
+            out.extend(np.asarray(transfers[s][r0:r0 + pts], dtype=np.complex64).reshape(-1))
+        r0 += pts
+    return np.array(out, dtype=np.complex64)
+
+
+def test_transfer_section_layout_matches_results_bin(tmp_path):
+    from wavey_gb300.wave import layout_transfers, write_transfer_section
+
+    rng = np.random.default_rng(7)
+    S, n_mics, planes, nf = 3, 2, [4, 5], 6
+    R = n_mics + sum(planes)
+    t = rng.normal(size=(S, R, nf)) + 1j * rng.normal(size=(S, R, nf))
+    sec = layout_transfers(t, n_mics, planes)
+    assert np.array_equal(sec, _save_layout_like_reference(t, n_mics, planes))
+    write_transfer_section(tmp_path / "t.bin", sec)
+    raw = np.fromfile(tmp_path / "t.bin", dtype="<f4")
+    assert np.array_equal(raw[0::2], sec.real) and np.array_equal(raw[1::2], sec.imag)
+
+
+def test_transfer_factors_reproduce_the_host_combination():
+    """The device combination's inputs: sum over lanes of factor x spectrum
+    equals the wave stage's host combination."""
+    from wavey_gb300.fdtd import source_signal
+    from wavey_gb300.wave import transfer_factors
+
+    room, g, speakers, rx, freqs, steps, _ = small_solve()
+    b = OracleBackend()
+    host = wave_stage(b, g, speakers, rx, freqs, c, 354.0, steps)
+    plans = [plan_speaker(g, sp, freqs, c, 1, False) for sp in speakers]
+    sig = source_signal(354.0, g.dt, steps)
+    lanes, fac = transfer_factors(g, speakers, plans, freqs, c, sig)
+    spectra = b.run_batch(g, [t for p in plans for t in p.components], sig, rx, freqs)
+    for s in range(len(speakers)):
+        dev = sum(fac[k][None, :] * spectra[k] for k in range(len(lanes)) if lanes[k] == s)
+        assert worst_relative(host.transfers[s], dev) < 1e-12

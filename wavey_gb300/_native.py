@@ -130,6 +130,13 @@ class WaveyTuneResult(C.Structure):
     ]
 
 
+class WaveyTransferLayout(C.Structure):
+    _fields_ = [
+        ("n_speakers", C.c_int32), ("lane_speaker", C.POINTER(C.c_int32)), ("factor", C.POINTER(C.c_double)),
+        ("n_mics", C.c_int64), ("n_planes", C.c_int32), ("plane_points", C.POINTER(C.c_int64)),
+    ]
+
+
 PROGRESS_FN = C.CFUNCTYPE(None, C.c_double, C.c_void_p)
 
 _host = None
@@ -217,6 +224,8 @@ def cuda() -> C.CDLL:
         "wavey_cuda_plan_info": (C.c_int, [vp, C.POINTER(WaveyPlanInfo)]),
         "wavey_cuda_plan_destroy": (None, [vp]),
         "wavey_cuda_plan_autotune": (C.c_int, [vp, C.POINTER(WaveyTuneResult)]),
+        "wavey_cuda_plan_transfers": (C.c_int, [vp, C.POINTER(WaveyTransferLayout), C.POINTER(C.c_float),
+                                                C.c_size_t]),
         "wavey_cuda_fdtd_run_rooms": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, cancel_p,
                                                 PROGRESS_FN, vp]),
         "wavey_cuda_rooms_create": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, C.c_int32,

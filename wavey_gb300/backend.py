@@ -326,6 +326,26 @@ class Plan:
                 "candidates": [(r.cand_cfg[i], r.cand_zt[i], r.cand_branch[i], r.cand_step_us[i])
                                for i in range(r.candidates)]}
 
+    def transfers(self, lane_speaker, factors, n_mics: int, plane_points=()) -> np.ndarray:
+        """Per-speaker transfer functions combined on the device
+        (wavey_cuda_plan_transfers): complex64 in the results.bin transfer
+        layout, mics [mic][speaker][f] then per plane [speaker][point][f],
+        flattened.  lane_speaker: speaker of each right-hand side (-1: left
+        out); factors: complex [sources][nf]."""
+        ls = np.ascontiguousarray(lane_speaker, dtype=np.int32)
+        fac = np.ascontiguousarray(np.asarray(factors, dtype=np.complex128))
+        pp = np.ascontiguousarray(plane_points, dtype=np.int64)
+        S = max(int(ls.max()) + 1, 0) if ls.size else 0
+        info = self.info()
+        out = np.zeros(int(info["receivers"]) * int(info["freqs"]) * S, dtype=np.complex64)
+        lay = N.WaveyTransferLayout(S, N.ptr(ls, C.c_int32), N.ptr(fac.view(np.float64), C.c_double), int(n_mics),
+                                    len(pp), N.ptr(pp, C.c_int64) if len(pp) else None)
+        with self._b._lock:
+            self._b._check(self._b._lib.wavey_cuda_plan_transfers(self._h, C.byref(lay),
+                                                                  N.ptr(out.view(np.float32), C.c_float),
+                                                                  2 * out.size))
+        return out
+
     def info(self) -> dict:
         i = N.WaveyPlanInfo()
         self._b._lib.wavey_cuda_plan_info(self._h, C.byref(i))

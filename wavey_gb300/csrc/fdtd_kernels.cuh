@@ -512,6 +512,47 @@ __global__ void ir_chunk(const T *ring, T *ir, int n_recv, int chunks, int n_sou
     ir[((long long)s * n_recv + r) * steps + *base + t] = ring[(((long long)c * RING + t) * n_recv + r) * V + l];
 }
 
+// Per-speaker transfer functions from a plan's spectra accumulators, as
+// complex64 in the results.bin transfer layout (result.rs:444-456): mics
+// [m][speaker][f], then per plane [speaker][point][f].  One thread per
+// (speaker, receiver, frequency): the sum over the speaker's right-hand sides
+// of factor[lane][f] x acc[lane][r][f] in FP64 (the factor carries the
+// component weight, the to_transfer scale and the calibration), rounded once
+// to FP32.  acc is [chunk][r][f][lane in chunk][2]; plane_first[p] is the
+// first receiver of plane p (plane_first[0] = n_mics, plane_first[n_planes] =
+// n_recv).
+__global__ void __launch_bounds__(BLOCK) speaker_transfers(const double *acc, int n_recv, int nf, int V,
+                                                           const int *spk_start, const int *spk_lanes,
+                                                           const double2 *factor, int n_speakers,
+                                                           const long long *plane_first, int n_planes, float2 *out) {
+    const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    const long long per_spk = (long long)n_recv * nf;
+    if (idx >= per_spk * n_speakers) return;
+    const int s = (int)(idx / per_spk);
+    const long long rf = idx - (long long)s * per_spk;
+    const int r = (int)(rf / nf), f = (int)(rf - (long long)r * nf);
+    double re = 0.0, im = 0.0;
+    for (int j = spk_start[s]; j < spk_start[s + 1]; j++) {
+        const int lane = spk_lanes[j];
+        const int c = lane / V, l = lane - c * V;
+        const double *a = acc + ((((long long)c * n_recv + r) * nf + f) * V + l) * 2;
+        const double2 k = factor[(long long)lane * nf + f];
+        re += k.x * a[0] - k.y * a[1];
+        im += k.x * a[1] + k.y * a[0];
+    }
+    const long long n_mics = plane_first[0];
+    long long o;
+    if (r < n_mics) {
+        o = ((long long)r * n_speakers + s) * nf + f;
+    } else {
+        int p = 0;
+        while (p + 1 < n_planes && r >= plane_first[p + 1]) p++;
+        const long long first = plane_first[p], points = plane_first[p + 1] - first;
+        o = n_mics * n_speakers * nf + (first - n_mics) * n_speakers * nf + ((long long)s * points + (r - first)) * nf + f;
+    }
+    out[o] = make_float2((float)re, (float)im);
+}
+
 __global__ void advance_base(long long *base, int by) { *base += by; }
 
 }  // namespace wk

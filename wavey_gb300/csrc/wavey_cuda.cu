@@ -1075,6 +1075,68 @@ int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progres
     return WAVEY_OK;
 }
 
+int plan_transfers(wavey_cuda_plan *pl, const wavey_transfer_layout *L, float *out, size_t out_floats) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    if (!L || !out) return ctx->fail(WAVEY_E_INVALID, "layout or out is null");
+    if (!pl->ran) return ctx->fail(WAVEY_E_INVALID, "the plan has not run");
+    const int S = L->n_speakers;
+    const int64_t R = pl->n_recv, F = pl->nf;
+    if (S <= 0 || !L->lane_speaker || !L->factor) return ctx->fail(WAVEY_E_INVALID, "no speakers or factors");
+    if (L->n_mics < 0 || L->n_planes < 0 || (L->n_planes > 0 && !L->plane_points))
+        return ctx->fail(WAVEY_E_INVALID, "bad receiver layout");
+    std::vector<long long> first(1, (long long)L->n_mics);
+    for (int p = 0; p < L->n_planes; p++) {
+        if (L->plane_points[p] < 0) return ctx->fail(WAVEY_E_INVALID, "negative plane size");
+        first.push_back(first.back() + L->plane_points[p]);
+    }
+    if (first.back() != R) return ctx->fail(WAVEY_E_INVALID, "mics and plane points (%lld) are not the plan's %lld receivers",
+                                            (long long)first.back(), (long long)R);
+    if (L->n_planes == 0) first.push_back(R);  // one empty plane keeps the kernel's search simple
+    if (out_floats != (size_t)(2 * R * F * S)) return ctx->fail(WAVEY_E_INVALID, "out holds %zu floats, not %lld", out_floats,
+                                                               (long long)(2 * R * F * S));
+    std::vector<int> start(S + 1, 0), lanes;
+    for (int s = 0; s < S; s++) {
+        for (int l = 0; l < pl->n_sources; l++) {
+            const int32_t k = L->lane_speaker[l];
+            if (k < -1 || k >= S) return ctx->fail(WAVEY_E_INVALID, "lane %d names speaker %d of %d", l, k, S);
+            if (k == s) lanes.push_back(l);
+        }
+        start[s + 1] = (int)lanes.size();
+    }
+    if (lanes.empty()) lanes.push_back(0);
+    cudaStream_t st0 = ctx->stream;
+    void *d_start = nullptr, *d_lanes = nullptr, *d_fac = nullptr, *d_first = nullptr, *d_out = nullptr;
+    const size_t fac_bytes = (size_t)pl->n_sources * F * 2 * sizeof(double), out_bytes = out_floats * sizeof(float);
+    auto release = [&]() {
+        for (void *q : {d_start, d_lanes, d_fac, d_first, d_out})
+            if (q) cudaFree(q);
+    };
+    int st;
+    if ((st = ctx->cuda(cudaMalloc(&d_start, start.size() * sizeof(int)), "alloc")) ||
+        (st = ctx->cuda(cudaMalloc(&d_lanes, lanes.size() * sizeof(int)), "alloc")) ||
+        (st = ctx->cuda(cudaMalloc(&d_fac, fac_bytes), "alloc")) ||
+        (st = ctx->cuda(cudaMalloc(&d_first, first.size() * sizeof(long long)), "alloc")) ||
+        (st = ctx->cuda(cudaMalloc(&d_out, out_bytes), "alloc"))) {
+        release();
+        return st;
+    }
+    cudaMemcpyAsync(d_start, start.data(), start.size() * sizeof(int), cudaMemcpyHostToDevice, st0);
+    cudaMemcpyAsync(d_lanes, lanes.data(), lanes.size() * sizeof(int), cudaMemcpyHostToDevice, st0);
+    cudaMemcpyAsync(d_fac, L->factor, fac_bytes, cudaMemcpyHostToDevice, st0);
+    cudaMemcpyAsync(d_first, first.data(), first.size() * sizeof(long long), cudaMemcpyHostToDevice, st0);
+    const long long total = (long long)S * R * F;
+    const int n_planes = std::max(L->n_planes, 1);
+    if (total > 0)
+        wk::speaker_transfers<<<(unsigned)((total + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, st0>>>(
+            pl->acc, (int)R, (int)F, pl->V, (const int *)d_start, (const int *)d_lanes, (const double2 *)d_fac, S,
+            (const long long *)d_first, n_planes, (float2 *)d_out);
+    st = ctx->cuda(cudaGetLastError(), "transfers launch");
+    if (!st) st = ctx->cuda(cudaMemcpyAsync(out, d_out, out_bytes, cudaMemcpyDeviceToHost, st0), "read transfers");
+    if (!st) st = ctx->cuda(cudaStreamSynchronize(st0), "transfers");
+    release();
+    return st;
+}
+
 int plan_read(wavey_cuda_plan *pl, double *out, double *ir_out) {
     wavey_cuda_ctx *ctx = pl->ctx;
     if (!pl->ran) return ctx->fail(WAVEY_E_INVALID, "the plan has not run");
@@ -1407,6 +1469,14 @@ int wavey_cuda_plan_autotune(wavey_cuda_plan *plan, wavey_tune_result *result) {
     std::lock_guard<std::mutex> lock(plan->ctx->mu);
     cudaSetDevice(plan->ctx->device);
     return plan_autotune(plan, result);
+}
+
+int wavey_cuda_plan_transfers(wavey_cuda_plan *plan, const wavey_transfer_layout *layout, float *out,
+                              size_t out_floats) {
+    if (!plan) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(plan->ctx->mu);
+    cudaSetDevice(plan->ctx->device);
+    return plan_transfers(plan, layout, out, out_floats);
 }
 
 int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {

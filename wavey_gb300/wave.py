@@ -254,3 +254,69 @@ def wave_stage(backend, grid: FdtdGrid, speakers, receivers, freqs, c: float, gr
         transfers.append(t)
         notes.extend(p.notes)
     return WaveStageResult(transfers, notes, len(sources), signal)
+
+
+# ------------------------------------------------------------------ results.bin
+def transfer_factors(grid: FdtdGrid, speakers, plans, freqs, c: float, signal, calibrations=None):
+    """Per right-hand side (in the batched run's order): its speaker and the
+    complex factor per frequency that maps its spectrum to its share of the
+    speaker's transfer -- component weight x to_transfer's scale
+    (fdtd.rs:819-840, evaluated on a unit spectrum) / cabinet calibration."""
+    calibrations = calibrations or {}
+    freqs = np.asarray(freqs, dtype=np.float64)
+    lane_speaker, factors = [], []
+    for s, (sp, p) in enumerate(zip(speakers, plans)):
+        unit = to_transfer(np.ones((1, len(freqs)), dtype=np.complex128), signal, grid, freqs, c,
+                           sp.reference_distance, _h0(sp, freqs))[0]
+        cal = calibrations.get(sp.name)
+        if cal is not None:
+            unit = unit / cal.on_axis
+        for ci in range(len(p.components)):
+            lane_speaker.append(s)
+            factors.append(p.weights[:, ci] * unit)
+    return np.array(lane_speaker, dtype=np.int32), np.array(factors, dtype=np.complex128)
+
+
+def layout_transfers(transfers, n_mics: int, plane_points) -> np.ndarray:
+    """Host-side form of the results.bin transfer section (result.rs:444-456)
+    from per-speaker transfers [speaker][receiver][f]: mics [mic][speaker][f],
+    then per plane [speaker][point][f], flattened complex64."""
+    t = np.asarray(transfers)
+    parts = [np.transpose(t[:, :n_mics, :], (1, 0, 2)).reshape(-1)]
+    r0 = n_mics
+    for pts in plane_points:
+        parts.append(t[:, r0:r0 + pts, :].reshape(-1))
+        r0 += pts
+    return np.concatenate(parts).astype(np.complex64)
+
+
+def wave_stage_results(backend, grid: FdtdGrid, speakers, receivers, n_mics: int, plane_points, freqs, c: float,
+                       grid_fmax: float, steps: int, source_order: int = 1, calibrations: dict | None = None,
+                       precision=FP32, cancel=None, progress=None, autotune: bool = False):
+    """The wave stage straight to the results.bin transfer section: the
+    batched run stays on the device as a plan, the per-speaker combination
+    runs on the device (wavey_cuda_plan_transfers) and only the complex64
+    result is read back.  receivers: the mics' nodes then every plane's
+    inside points' nodes, in plane order.  Returns the flattened section (see
+    layout_transfers), or None if cancelled."""
+    calibrations = calibrations or {}
+    freqs = np.asarray(freqs, dtype=np.float64)
+    signal = source_signal(grid_fmax, grid.dt, steps)
+    plans = [plan_speaker(grid, sp, freqs, c, source_order, sp.name in calibrations) for sp in speakers]
+    sources = [t for p in plans for t in p.components]
+    lane_speaker, factors = transfer_factors(grid, speakers, plans, freqs, c, signal, calibrations)
+    plan = backend.plan(grid, sources, signal, receivers, freqs, precision)
+    try:
+        if autotune:
+            plan.autotune()
+        if plan.run(cancel=cancel, progress=progress) is None:
+            return None
+        return plan.transfers(lane_speaker, factors, n_mics, plane_points)
+    finally:
+        plan.close()
+
+
+def write_transfer_section(path, section: np.ndarray) -> None:
+    """Writes the transfer section as results.bin stores it: interleaved
+    little-endian f32 (re, im) pairs."""
+    np.ascontiguousarray(section, dtype=np.complex64).astype("<c8").tofile(path)
