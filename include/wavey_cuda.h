@@ -155,6 +155,27 @@ typedef struct {
 int wavey_cuda_plan_transfers(wavey_cuda_plan *plan, const wavey_transfer_layout *layout, float *out,
                               size_t out_floats);
 
+/* ISO 3382-1 band parameters of a plan's receiver time series, computed on
+ * the device (core/wavey-solver/src/analysis.rs), for IR-mode plans
+ * (want_ir): per right-hand side, receiver and band -- octave band-pass
+ * (six biquads forward and backward, analysis.rs:143-183) of the series
+ * from the broadband onset (analysis.rs:185-189), Schroeder integration,
+ * EDT, T20, T30, C80, D50 and centre time (analysis.rs:266-325).  Only these
+ * numbers cross to the host, not the series.  Replaces reading the series
+ * (run_cpu_ir) and calling octave_filter / band_params per receiver and band
+ * on the host (bras_wave.rs:46-58); no counterpart call in the reference.
+ * flags: WAVEY_IR_INTEGRATE analyses the running sum of the series (the
+ * response to the source pulse's integral, bras_wave.rs:46-52);
+ * WAVEY_IR_LUNDEBY truncates and compensates the noise tail
+ * (energy_params, analysis.rs:291-294) instead of integrating all of it
+ * (noise_free_params).  out: [source][receiver][band][6] = edt, t20, t30 (s),
+ * c80 (dB), d50, ts (s); NaN where undefined.  1 to 64 bands, each below
+ * fs / 2 = 1 / (2 dt). */
+#define WAVEY_IR_INTEGRATE 1
+#define WAVEY_IR_LUNDEBY 2
+int wavey_cuda_plan_band_params(wavey_cuda_plan *plan, const double *bands_hz, int32_t n_bands, int32_t flags,
+                                double *out, size_t out_doubles);
+
 /* Autotuner of a plan's step kernels (FP32 plans of at least 256 steps).
  * Stage 1 times every shape of the interior kernel -- tile rows (8 or 16)
  * with ring depths, and z planes per CTA (8, 16, 32 and the runs that fill

@@ -14,11 +14,12 @@ OUT = HERE / "_build" / "libwavey_oracle.so"
 
 
 def build(force: bool = False) -> Path:
-    src = HERE / "fdtd_oracle.c"
-    if not force and OUT.exists() and OUT.stat().st_mtime >= src.stat().st_mtime:
+    srcs = [HERE / "fdtd_oracle.c", HERE / "ir_oracle.c"]
+    if not force and OUT.exists() and all(OUT.stat().st_mtime >= s.stat().st_mtime for s in srcs):
         return OUT
     OUT.parent.mkdir(exist_ok=True)
-    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", str(src), "-o", str(OUT), "-lm"]
+    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", *map(str, srcs), "-o", str(OUT),
+           "-lm"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{res.stderr}")

@@ -119,6 +119,8 @@ class WaveyPlanInfo(C.Structure):
 
 
 WAVEY_TUNE_MAX = 64
+WAVEY_IR_INTEGRATE = 1
+WAVEY_IR_LUNDEBY = 2
 
 
 class WaveyTuneResult(C.Structure):
@@ -226,6 +228,7 @@ def cuda() -> C.CDLL:
         "wavey_cuda_plan_autotune": (C.c_int, [vp, C.POINTER(WaveyTuneResult)]),
         "wavey_cuda_plan_transfers": (C.c_int, [vp, C.POINTER(WaveyTransferLayout), C.POINTER(C.c_float),
                                                 C.c_size_t]),
+        "wavey_cuda_plan_band_params": (C.c_int, [vp, c_double_p, C.c_int32, C.c_int32, c_double_p, C.c_size_t]),
         "wavey_cuda_fdtd_run_rooms": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, cancel_p,
                                                 PROGRESS_FN, vp]),
         "wavey_cuda_rooms_create": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, C.c_int32,

@@ -346,6 +346,20 @@ class Plan:
                                                                   2 * out.size))
         return out
 
+    def band_params(self, bands=(63.0, 125.0, 250.0, 500.0, 1000.0, 2000.0, 4000.0, 8000.0), integrate: bool = True,
+                    lundeby: bool = False) -> np.ndarray:
+        """ISO 3382-1 parameters of every receiver's time series, computed on
+        the device (wavey_cuda_plan_band_params; IR plans only):
+        [source][receiver][band][6] = edt, t20, t30, c80, d50, ts."""
+        b = np.ascontiguousarray(bands, dtype=np.float64)
+        info = self.info()
+        out = np.zeros((int(info["sources"]), int(info["receivers"]), len(b), 6))
+        flags = (N.WAVEY_IR_INTEGRATE if integrate else 0) | (N.WAVEY_IR_LUNDEBY if lundeby else 0)
+        with self._b._lock:
+            self._b._check(self._b._lib.wavey_cuda_plan_band_params(self._h, N.ptr(b, C.c_double), len(b), flags,
+                                                                    N.ptr(out, C.c_double), out.size))
+        return out
+
     def info(self) -> dict:
         i = N.WaveyPlanInfo()
         self._b._lib.wavey_cuda_plan_info(self._h, C.byref(i))

@@ -31,6 +31,7 @@
 #include "fdtd_half.cuh"
 #include "fdtd_kernels.cuh"
 #include "interior_tma.cuh"
+#include "ir_analysis.cuh"
 
 namespace {
 
@@ -1137,6 +1138,68 @@ int plan_transfers(wavey_cuda_plan *pl, const wavey_transfer_layout *L, float *o
     return st;
 }
 
+int plan_band_params(wavey_cuda_plan *pl, const double *bands, int32_t nb, int32_t flags, double *out,
+                     size_t out_doubles) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    if (!bands || !out) return ctx->fail(WAVEY_E_INVALID, "bands or out is null");
+    if (!pl->ran) return ctx->fail(WAVEY_E_INVALID, "the plan has not run");
+    if (!pl->want_ir) return ctx->fail(WAVEY_E_INVALID, "the plan records no time series");
+    if (nb < 1 || nb > 64) return ctx->fail(WAVEY_E_INVALID, "1 to 64 bands");
+    if (flags & ~(wk::IR_INTEGRATE | wk::IR_LUNDEBY)) return ctx->fail(WAVEY_E_INVALID, "unknown flags %d", flags);
+    const double fs = 1.0 / pl->dt;
+    for (int b = 0; b < nb; b++)
+        if (!(bands[b] > 0.0 && bands[b] < 0.5 * fs)) return ctx->fail(WAVEY_E_INVALID, "band %g Hz is not below fs / 2", bands[b]);
+    const long long series = (long long)pl->n_sources * pl->n_recv, steps = (long long)pl->steps;
+    if (out_doubles != (size_t)(series * nb * 6)) return ctx->fail(WAVEY_E_INVALID, "out holds %zu doubles, not %lld",
+                                                                   out_doubles, series * nb * 6);
+    if (series == 0 || steps == 0) return WAVEY_OK;
+    // Scratch of one launch: a band-passed series per thread; launches take
+    // whole series, as many as 2 GiB (or half the free memory) holds.
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t budget = std::min<size_t>((size_t)2 << 30, free_b / 2);
+    const long long per_series = (long long)nb * steps * (long long)sizeof(double);
+    const long long batch = std::max(1LL, std::min(series, (long long)(budget / (size_t)per_series)));
+    cudaStream_t st0 = ctx->stream;
+    void *d_onset = nullptr, *d_bands = nullptr, *d_out = nullptr, *d_scratch = nullptr;
+    auto release = [&]() {
+        for (void *q : {d_onset, d_bands, d_out, d_scratch})
+            if (q) cudaFree(q);
+    };
+    int st;
+    if ((st = ctx->cuda(cudaMalloc(&d_onset, series * sizeof(long long)), "alloc")) ||
+        (st = ctx->cuda(cudaMalloc(&d_bands, nb * sizeof(double)), "alloc")) ||
+        (st = ctx->cuda(cudaMalloc(&d_out, out_doubles * sizeof(double)), "alloc")) ||
+        (st = ctx->cuda(cudaMalloc(&d_scratch, (size_t)(batch * per_series)), "alloc scratch"))) {
+        release();
+        return st;
+    }
+    cudaMemcpyAsync(d_bands, bands, nb * sizeof(double), cudaMemcpyHostToDevice, st0);
+    const unsigned ob = (unsigned)((series + 127) / 128);
+    if (pl->precision == WAVEY_FP64)
+        wk::ir_onsets<double><<<ob, 128, 0, st0>>>((const double *)pl->ir, steps, series, flags, (long long *)d_onset);
+    else
+        wk::ir_onsets<float><<<ob, 128, 0, st0>>>((const float *)pl->ir, steps, series, flags, (long long *)d_onset);
+    for (long long first = 0; first < series && !st; first += batch) {
+        const long long n = std::min(batch, series - first);
+        const unsigned blocks = (unsigned)((n * nb + 127) / 128);
+        if (pl->precision == WAVEY_FP64)
+            wk::ir_band_params<double><<<blocks, 128, 0, st0>>>((const double *)pl->ir, steps, (const long long *)d_onset,
+                                                                first, n, (const double *)d_bands, nb, fs, flags,
+                                                                (double *)d_scratch, (double *)d_out);
+        else
+            wk::ir_band_params<float><<<blocks, 128, 0, st0>>>((const float *)pl->ir, steps, (const long long *)d_onset,
+                                                               first, n, (const double *)d_bands, nb, fs, flags,
+                                                               (double *)d_scratch, (double *)d_out);
+        st = ctx->cuda(cudaGetLastError(), "band parameters launch");
+    }
+    if (!st) st = ctx->cuda(cudaMemcpyAsync(out, d_out, out_doubles * sizeof(double), cudaMemcpyDeviceToHost, st0),
+                            "read band parameters");
+    if (!st) st = ctx->cuda(cudaStreamSynchronize(st0), "band parameters");
+    release();
+    return st;
+}
+
 int plan_read(wavey_cuda_plan *pl, double *out, double *ir_out) {
     wavey_cuda_ctx *ctx = pl->ctx;
     if (!pl->ran) return ctx->fail(WAVEY_E_INVALID, "the plan has not run");
@@ -1477,6 +1540,14 @@ int wavey_cuda_plan_transfers(wavey_cuda_plan *plan, const wavey_transfer_layout
     std::lock_guard<std::mutex> lock(plan->ctx->mu);
     cudaSetDevice(plan->ctx->device);
     return plan_transfers(plan, layout, out, out_floats);
+}
+
+int wavey_cuda_plan_band_params(wavey_cuda_plan *plan, const double *bands_hz, int32_t n_bands, int32_t flags,
+                                double *out, size_t out_doubles) {
+    if (!plan) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(plan->ctx->mu);
+    cudaSetDevice(plan->ctx->device);
+    return plan_band_params(plan, bands_hz, n_bands, flags, out, out_doubles);
 }
 
 int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
