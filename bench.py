@@ -245,8 +245,26 @@ def run_ours(args, rank, world):
             raise SystemExit(f"room_hall needs about {need / 1e9:.0f} GB of device memory, {free / 1e9:.0f} GB free")
         args.no_plain = args.no_e2e_big = True
         args.no_accuracy = args.no_cpu = args.no_autotune = True
+        args.grid_build = True
     S = len(scene.sources)
     b = CudaBackend(dev)
+    grid_build = None
+    if getattr(args, "grid_build", False):
+        # The grid build on the host (wh_grid_build, OpenMP) and on the device
+        # (wavey_cuda_grid_build, arrays read back), identical arrays.
+        from wavey_gb300.fdtd import FdtdGrid
+
+        t0 = time.perf_counter()
+        FdtdGrid.build_dx(scene.room, scene.fits, W.C_AIR, g.dx)
+        t1 = time.perf_counter()
+        gd = b.build_grid(scene.room, scene.fits, W.C_AIR, g.dx)
+        t2 = time.perf_counter()
+        same = bool(np.array_equal(gd.flags, g.flags) and np.array_equal(gd.slots, g.slots)
+                    and np.array_equal(gd.bidx, g.bidx))
+        del gd
+        grid_build = {"cells": g.cells, "host_s": t1 - t0, "device_s": t2 - t1, "identical": same,
+                      "host_threads": os.cpu_count()}
+        log(f"[rank {rank}] grid build: host {t1 - t0:.2f} s, device {t2 - t1:.2f} s, identical {same}")
     name, sms = b.device_info()
     log(f"[rank {rank}] {name} ({sms} SMs): {scene.name} grid {g.n}, air {g.air}, {scene.steps} steps, S={S}, "
         f"{len(scene.receivers)} receivers x {len(scene.freqs)} bins")
@@ -408,6 +426,7 @@ def run_ours(args, rank, world):
                     "d2h_bytes_per_step": info["d2h_bytes"], "seconds": e2e_s},
             "accuracy": acc,
             "fp16_storage": fp16,
+            "grid_build": grid_build,
             "cpu_baseline": cpu,
             "gpu_launches": int(kernels_per_run * args.steps),
             "clocks": clocks.summary(),

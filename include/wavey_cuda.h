@@ -29,6 +29,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "wavey_host.h"
+
 #include "wavey_status.h"
 
 #ifdef __cplusplus
@@ -175,6 +177,28 @@ int wavey_cuda_plan_transfers(wavey_cuda_plan *plan, const wavey_transfer_layout
 #define WAVEY_IR_LUNDEBY 2
 int wavey_cuda_plan_band_params(wavey_cuda_plan *plan, const double *bands_hz, int32_t n_bands, int32_t flags,
                                 double *out, size_t out_doubles);
+
+/* FdtdGrid::build_dx (fdtd.rs:289-378) on the device: the same
+ * classification, neighbour flags, face lookup and boundary slots as
+ * wh_grid_build, computed per cell on the GPU (boundary nodes numbered in
+ * cell order by a scan), for rooms whose host build takes seconds (the
+ * 376 M-cell hall).  The arrays are identical to wh_grid_build's.  Two
+ * steps: wavey_cuda_grid_build leaves the grid on the device and reports its
+ * shape; wavey_cuda_grid_read copies it into host arrays of that shape (e.g.
+ * those of wh_grid_alloc / wh_grid_arrays).  No counterpart in the
+ * reference, whose grid build is CPU-only. */
+typedef struct wavey_device_grid wavey_device_grid;
+typedef struct {
+    int64_t n[3];
+    double origin[3];
+    double dx, dt;
+    int64_t air_cells, n_boundary, n_slots;
+} wavey_grid_shape;
+int wavey_cuda_grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int32_t n_fits, double c,
+                          double dx, wavey_device_grid **out, wavey_grid_shape *shape);
+int wavey_cuda_grid_read(wavey_device_grid *grid, uint8_t *flags, uint32_t *bidx, uint32_t *bcell, uint32_t *bstart,
+                         double *slots);
+void wavey_cuda_grid_free(wavey_device_grid *grid);
 
 /* Autotuner of a plan's step kernels (FP32 plans of at least 256 steps).
  * Stage 1 times every shape of the interior kernel -- tile rows (8 or 16)

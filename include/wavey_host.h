@@ -113,6 +113,15 @@ int wh_grid_build(const wh_room *room, const wh_fit *fits, int32_t n_fits, doubl
 double wh_grid_spacing(const wh_room *room, double c, double f_max, double ppw);
 void wh_grid_view_of(const wh_grid *g, wh_grid_view *out);
 void wh_grid_free(wh_grid *g);
+/* An empty grid of the given shape with room for n_boundary nodes and
+ * n_slots slots, for a builder outside this library to fill (the CUDA grid
+ * builder, wavey_cuda_grid_build / wavey_cuda_grid_read): flags zeroed, bidx
+ * WAVEY_NO_BOUNDARY; wh_grid_arrays gives the writable arrays.  No
+ * counterpart in the reference. */
+int wh_grid_alloc(const int64_t n[3], const double origin[3], double dx, double dt, int64_t air_cells,
+                  int64_t n_boundary, int64_t n_slots, wh_grid **out);
+void wh_grid_arrays(wh_grid *g, uint8_t **flags, uint32_t **bidx, uint32_t **bcell, uint32_t **bstart,
+                    double **slots);
 
 /* fdtd.rs:245-272; returns the cell or -1. */
 int64_t wh_nearest_air(const wh_grid *g, const double p[3]);

@@ -139,6 +139,11 @@ class WaveyTransferLayout(C.Structure):
     ]
 
 
+class WaveyGridShape(C.Structure):
+    _fields_ = [("n", C.c_int64 * 3), ("origin", C.c_double * 3), ("dx", C.c_double), ("dt", C.c_double),
+                ("air_cells", C.c_int64), ("n_boundary", C.c_int64), ("n_slots", C.c_int64)]
+
+
 PROGRESS_FN = C.CFUNCTYPE(None, C.c_double, C.c_void_p)
 
 _host = None
@@ -172,6 +177,11 @@ def host() -> C.CDLL:
         "wh_grid_spacing": (C.c_double, [C.POINTER(WhRoom), C.c_double, C.c_double, C.c_double]),
         "wh_grid_view_of": (None, [C.c_void_p, C.POINTER(WhGridView)]),
         "wh_grid_free": (None, [C.c_void_p]),
+        "wh_grid_alloc": (C.c_int, [c_int64_p, c_double_p, C.c_double, C.c_double, C.c_int64, C.c_int64, C.c_int64,
+                                    C.POINTER(C.c_void_p)]),
+        "wh_grid_arrays": (None, [C.c_void_p, C.POINTER(C.POINTER(C.c_uint8)), C.POINTER(C.POINTER(C.c_uint32)),
+                                  C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.POINTER(C.c_uint32)),
+                                  C.POINTER(C.POINTER(C.c_double))]),
         "wh_nearest_air": (C.c_int64, [C.c_void_p, c_double_p]),
         "wh_taps_at": (C.c_int32, [C.c_void_p, c_double_p, c_int64_p, c_double_p]),
         "wh_source_components": (C.c_int32, [C.c_void_p, C.c_int64, C.c_int32, c_int64_p, c_double_p,
@@ -229,6 +239,11 @@ def cuda() -> C.CDLL:
         "wavey_cuda_plan_transfers": (C.c_int, [vp, C.POINTER(WaveyTransferLayout), C.POINTER(C.c_float),
                                                 C.c_size_t]),
         "wavey_cuda_plan_band_params": (C.c_int, [vp, c_double_p, C.c_int32, C.c_int32, c_double_p, C.c_size_t]),
+        "wavey_cuda_grid_build": (C.c_int, [vp, C.POINTER(WhRoom), C.POINTER(WhFit), C.c_int32, C.c_double, C.c_double,
+                                            C.POINTER(vp), C.POINTER(WaveyGridShape)]),
+        "wavey_cuda_grid_read": (C.c_int, [vp, C.POINTER(C.c_uint8), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                           C.POINTER(C.c_uint32), c_double_p]),
+        "wavey_cuda_grid_free": (None, [vp]),
         "wavey_cuda_fdtd_run_rooms": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, cancel_p,
                                                 PROGRESS_FN, vp]),
         "wavey_cuda_rooms_create": (C.c_int, [vp, C.POINTER(WaveyRoomJob), C.c_size_t, C.c_int32, C.c_int32,

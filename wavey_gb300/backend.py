@@ -160,6 +160,35 @@ class CudaBackend:
             return None
         return (out, irbuf) if ir else out
 
+    def build_grid(self, room, fits, c: float, dx: float):
+        """FdtdGrid.build_dx on the device (wavey_cuda_grid_build): the same
+        arrays as the host builder, returned as an FdtdGrid."""
+        from .fdtd import FdtdGrid
+
+        if len(fits) != room.n_surfaces:
+            raise ValueError(f"{len(fits)} fits for {room.n_surfaces} surfaces")
+        r, keep = room._c()
+        arr = (N.WhFit * len(fits))(*[f._c() for f in fits])
+        dg, sh = C.c_void_p(), N.WaveyGridShape()
+        with self._lock:
+            self._check(self._lib.wavey_cuda_grid_build(self._h, C.byref(r), arr, len(fits), float(c), float(dx),
+                                                        C.byref(dg), C.byref(sh)))
+        try:
+            out = C.c_void_p()
+            st = N.host().wh_grid_alloc(sh.n, sh.origin, sh.dx, sh.dt, sh.air_cells, sh.n_boundary, sh.n_slots,
+                                        C.byref(out))
+            if st != 0:
+                raise WaveyError(st, "host grid allocation failed")
+            p = [C.POINTER(C.c_uint8)(), C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint32)(),
+                 C.POINTER(C.c_double)()]
+            N.host().wh_grid_arrays(out, *[C.byref(q) for q in p])
+            grid = FdtdGrid(out.value)  # owns the host arrays from here
+            with self._lock:
+                self._check(self._lib.wavey_cuda_grid_read(dg, *p))
+            return grid
+        finally:
+            self._lib.wavey_cuda_grid_free(dg)
+
     def plan(self, grid, sources, signal, receivers, freqs, precision=FP32, ir: bool = False) -> "Plan":
         return Plan(self, grid, sources, signal, receivers, freqs, precision, ir)
 

@@ -354,6 +354,46 @@ extern "C" void wh_grid_view_of(const wh_grid *g, wh_grid_view *v) {
 
 extern "C" void wh_grid_free(wh_grid *g) { delete g; }
 
+extern "C" int wh_grid_alloc(const int64_t n[3], const double origin[3], double dx, double dt, int64_t air_cells,
+                             int64_t n_boundary, int64_t n_slots, wh_grid **out) {
+    if (!n || !origin || !out || n[0] < 3 || n[1] < 3 || n[2] < 3 || n_boundary < 0 || n_slots < 0 ||
+        n_boundary >= (int64_t)WAVEY_NO_BOUNDARY)
+        return WAVEY_E_INVALID;
+    const uint64_t cells = (uint64_t)n[0] * (uint64_t)n[1] * (uint64_t)n[2];
+    if (cells > WAVEY_MAX_CELLS) return WAVEY_E_LIMIT;
+    *out = nullptr;
+    wh_grid *g = new (std::nothrow) wh_grid();
+    if (!g) return WAVEY_E_NOMEM;
+    for (int a = 0; a < 3; a++) {
+        g->n[a] = n[a];
+        g->origin[a] = origin[a];
+    }
+    g->dx = dx;
+    g->dt = dt;
+    g->air = air_cells;
+    try {
+        g->flags.assign(cells, 0);
+        g->bidx.assign(cells, WAVEY_NO_BOUNDARY);
+        g->bcell.assign((size_t)n_boundary, 0);
+        g->bstart.assign((size_t)n_boundary + 1, 0);
+        g->slots.assign((size_t)n_slots * 4, 0.0);
+    } catch (...) {
+        delete g;
+        return WAVEY_E_NOMEM;
+    }
+    *out = g;
+    return WAVEY_OK;
+}
+
+extern "C" void wh_grid_arrays(wh_grid *g, uint8_t **flags, uint32_t **bidx, uint32_t **bcell, uint32_t **bstart,
+                               double **slots) {
+    *flags = g->flags.data();
+    *bidx = g->bidx.data();
+    *bcell = g->bcell.data();
+    *bstart = g->bstart.data();
+    *slots = g->slots.data();
+}
+
 extern "C" int64_t wh_nearest_air(const wh_grid *g, const double p[3]) {
     int64_t c[3];
     for (int a = 0; a < 3; a++) c[a] = (int64_t)std::round((p[a] - g->origin[a]) / g->dx);

@@ -32,6 +32,7 @@
 #include "fdtd_kernels.cuh"
 #include "interior_tma.cuh"
 #include "ir_analysis.cuh"
+#include "grid_build.cuh"
 
 namespace {
 
@@ -167,6 +168,15 @@ struct wavey_cuda_plan {
 // Several rooms advanced together: their plans (buffers and packing), one
 // shared step counter, the device table of RoomStep entries and one graph per
 // 128-step chunk whose step launches cover every room's blocks.
+// A grid built on the device (wavey_cuda_grid_build).
+struct wavey_device_grid {
+    wavey_cuda_ctx *ctx = nullptr;
+    wavey_grid_shape shape{};
+    uint8_t *flags = nullptr;
+    uint32_t *bidx = nullptr, *bcell = nullptr, *bstart = nullptr;
+    double *slots = nullptr;
+};
+
 struct wavey_cuda_rooms {
     wavey_cuda_ctx *ctx = nullptr;
     int precision = WAVEY_FP32;
@@ -1200,6 +1210,176 @@ int plan_band_params(wavey_cuda_plan *pl, const double *bands, int32_t nb, int32
     return st;
 }
 
+// ---------------------------------------------------------------- grid build
+void free_device_grid(wavey_device_grid *g) {
+    if (!g) return;
+    for (void *q : {(void *)g->flags, (void *)g->bidx, (void *)g->bcell, (void *)g->bstart, (void *)g->slots})
+        if (q) cudaFree(q);
+    delete g;
+}
+
+// Surfaces in build_room order: floor, ceiling, walls y0, x1, y1, x0, then 4
+// faces per pillar and 6 per block (the host builder's list).
+std::vector<wk::GbRect> room_rects_of(const wh_room *r) {
+    std::vector<wk::GbRect> s;
+    auto add = [&](int axis, double c, double x0, double y0, double z0, double x1, double y1, double z1) {
+        wk::GbRect q;
+        q.axis = axis;
+        q.c = c;
+        q.lo[0] = x0, q.lo[1] = y0, q.lo[2] = z0;
+        q.hi[0] = x1, q.hi[1] = y1, q.hi[2] = z1;
+        s.push_back(q);
+    };
+    const double h = r->height;
+    add(2, 0.0, r->x0, r->y0, 0, r->x1, r->y1, 0);
+    add(2, h, r->x0, r->y0, 0, r->x1, r->y1, 0);
+    add(1, r->y0, r->x0, 0, 0.0, r->x1, 0, h);
+    add(0, r->x1, 0, r->y0, 0.0, 0, r->y1, h);
+    add(1, r->y1, r->x0, 0, 0.0, r->x1, 0, h);
+    add(0, r->x0, 0, r->y0, 0.0, 0, r->y1, h);
+    for (int i = 0; i < r->n_pillars; i++) {
+        const double *p = r->pillars + 4 * i;
+        add(1, p[1], p[0], 0, 0.0, p[2], 0, h);
+        add(0, p[0], 0, p[1], 0.0, 0, p[3], h);
+        add(1, p[3], p[0], 0, 0.0, p[2], 0, h);
+        add(0, p[2], 0, p[1], 0.0, 0, p[3], h);
+    }
+    for (int i = 0; i < r->n_blocks; i++) {
+        const double *b = r->blocks + 6 * i;
+        add(0, b[0], 0, b[1], b[2], 0, b[4], b[5]);
+        add(0, b[3], 0, b[1], b[2], 0, b[4], b[5]);
+        add(1, b[1], b[0], 0, b[2], b[3], 0, b[5]);
+        add(1, b[4], b[0], 0, b[2], b[3], 0, b[5]);
+        add(2, b[2], b[0], b[1], 0, b[3], b[4], 0);
+        add(2, b[5], b[0], b[1], 0, b[3], b[4], 0);
+    }
+    return s;
+}
+
+int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int32_t n_fits, double c, double dx,
+               wavey_device_grid **out, wavey_grid_shape *shape) {
+    if (!out || !shape) return ctx->fail(WAVEY_E_INVALID, "out or shape is null");
+    *out = nullptr;
+    if (!room || !(dx > 0.0) || !(c > 0.0) || !(room->height > 0.0) || room->x1 <= room->x0 || room->y1 <= room->y0)
+        return ctx->fail(WAVEY_E_INVALID, "invalid room or spacing");
+    if ((room->n_pillars > 0 && !room->pillars) || (room->n_blocks > 0 && !room->blocks) ||
+        (room->n_solids > 0 && !room->solids) || room->n_pillars < 0 || room->n_blocks < 0 || room->n_solids < 0)
+        return ctx->fail(WAVEY_E_INVALID, "invalid room lists");
+    const std::vector<wk::GbRect> rects = room_rects_of(room);
+    if ((int)rects.size() != n_fits || !fits) return ctx->fail(WAVEY_E_INVALID, "%d fits for %zu surfaces", n_fits, rects.size());
+    wavey_grid_shape sh{};
+    const double lo[3] = {room->x0, room->y0, 0.0}, hi[3] = {room->x1, room->y1, room->height};
+    sh.dx = dx;
+    sh.dt = WAVEY_COURANT * dx / c;
+    for (int a = 0; a < 3; a++) {
+        sh.origin[a] = lo[a] - dx * 0.5;
+        sh.n[a] = (int64_t)std::ceil((hi[a] - lo[a]) / dx) + 2;
+    }
+    const long long cells = (long long)sh.n[0] * sh.n[1] * sh.n[2];
+    if ((unsigned long long)cells > WAVEY_MAX_CELLS) return ctx->fail(WAVEY_E_LIMIT, "%lld cells > MAX_CELLS", cells);
+    cudaStream_t s = ctx->stream;
+    wavey_device_grid *g = new (std::nothrow) wavey_device_grid();
+    if (!g) return ctx->fail(WAVEY_E_NOMEM, "host allocation failed");
+    g->ctx = ctx;
+    std::vector<void *> tmp;
+    auto dalloc = [&](void **p, size_t bytes, bool keep) -> int {
+        int st = ctx->cuda(cudaMalloc(p, std::max<size_t>(bytes, 8)), "grid alloc");
+        if (!st && !keep) tmp.push_back(*p);
+        return st;
+    };
+    auto fail = [&](int st) {
+        for (void *q : tmp) cudaFree(q);
+        free_device_grid(g);
+        return st;
+    };
+    const long long nscan = (cells + wk::SCAN_BLOCK - 1) / wk::SCAN_BLOCK;
+    void *d_pill = nullptr, *d_blk = nullptr, *d_sol = nullptr, *d_rects = nullptr, *d_fits = nullptr, *d_solid = nullptr,
+         *d_air = nullptr, *d_cnt = nullptr, *d_air_n = nullptr, *d_ntot = nullptr, *d_stot = nullptr, *d_grand = nullptr,
+         *d_node_at = nullptr, *d_slot_at = nullptr;
+    int st;
+    if ((st = dalloc(&d_pill, sizeof(double) * 4 * room->n_pillars, false)) ||
+        (st = dalloc(&d_blk, sizeof(double) * 6 * room->n_blocks, false)) ||
+        (st = dalloc(&d_sol, sizeof(double) * 6 * room->n_solids, false)) ||
+        (st = dalloc(&d_rects, sizeof(wk::GbRect) * rects.size(), false)) ||
+        (st = dalloc(&d_fits, sizeof(wh_fit) * n_fits, false)) || (st = dalloc(&d_solid, cells, false)) ||
+        (st = dalloc(&d_air, cells, false)) || (st = dalloc(&d_cnt, 4 * (size_t)cells, false)) ||
+        (st = dalloc(&d_air_n, 8, false)) || (st = dalloc(&d_ntot, 8 * (size_t)nscan, false)) ||
+        (st = dalloc(&d_stot, 8 * (size_t)nscan, false)) || (st = dalloc(&d_grand, 16, false)) ||
+        (st = dalloc(&d_node_at, 4 * (size_t)cells, false)) || (st = dalloc(&d_slot_at, 8 * (size_t)cells, false)) ||
+        (st = dalloc((void **)&g->flags, cells, true)) || (st = dalloc((void **)&g->bidx, 4 * (size_t)cells, true)))
+        return fail(st);
+    if (room->n_pillars) cudaMemcpyAsync(d_pill, room->pillars, sizeof(double) * 4 * room->n_pillars, cudaMemcpyHostToDevice, s);
+    if (room->n_blocks) cudaMemcpyAsync(d_blk, room->blocks, sizeof(double) * 6 * room->n_blocks, cudaMemcpyHostToDevice, s);
+    if (room->n_solids) cudaMemcpyAsync(d_sol, room->solids, sizeof(double) * 6 * room->n_solids, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_rects, rects.data(), sizeof(wk::GbRect) * rects.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_fits, fits, sizeof(wh_fit) * n_fits, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(g->flags, 0, cells, s);
+    cudaMemsetAsync(g->bidx, 0xFF, 4 * (size_t)cells, s);
+    cudaMemsetAsync(d_air_n, 0, 8, s);
+    wk::GbRoom r;
+    r.x0 = room->x0, r.y0 = room->y0, r.x1 = room->x1, r.y1 = room->y1, r.height = room->height;
+    r.n_pillars = room->n_pillars, r.n_blocks = room->n_blocks, r.n_solids = room->n_solids;
+    r.n_rects = (int)rects.size();
+    r.pillars = (const double *)d_pill, r.blocks = (const double *)d_blk, r.solids = (const double *)d_sol;
+    r.rects = (const wk::GbRect *)d_rects;
+    r.fits = (const wh_fit *)d_fits;
+    r.nx = sh.n[0], r.ny = sh.n[1], r.nz = sh.n[2];
+    for (int a = 0; a < 3; a++) r.origin[a] = sh.origin[a];
+    r.dx = sh.dx, r.dt = sh.dt;
+    const unsigned blocks = (unsigned)((cells + 255) / 256);
+    wk::grid_classify<<<blocks, 256, 0, s>>>(r, (uint8_t *)d_solid, (uint8_t *)d_air);
+    wk::grid_flags<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_air, g->flags, (unsigned long long *)d_air_n);
+    wk::grid_nodes<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_solid, g->flags, (uint32_t *)d_cnt, false, nullptr,
+                                          nullptr, nullptr, nullptr, nullptr, nullptr);
+    wk::scan_totals<<<(unsigned)nscan, wk::SCAN_BLOCK, 0, s>>>((const uint32_t *)d_cnt, cells,
+                                                               (unsigned long long *)d_ntot, (unsigned long long *)d_stot);
+    wk::scan_block_totals<<<1, wk::SCAN_BLOCK, 0, s>>>((unsigned long long *)d_ntot, (unsigned long long *)d_stot, nscan,
+                                                       (unsigned long long *)d_grand);
+    wk::scan_apply<<<(unsigned)nscan, wk::SCAN_BLOCK, 0, s>>>((const uint32_t *)d_cnt, cells,
+                                                              (const unsigned long long *)d_ntot,
+                                                              (const unsigned long long *)d_stot, (uint32_t *)d_node_at,
+                                                              (unsigned long long *)d_slot_at);
+    unsigned long long grand[2] = {0, 0}, air_n = 0;
+    cudaMemcpyAsync(grand, d_grand, 16, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&air_n, d_air_n, 8, cudaMemcpyDeviceToHost, s);
+    if ((st = ctx->cuda(cudaStreamSynchronize(s), "grid build"))) return fail(st);
+    if (grand[0] >= (unsigned long long)WAVEY_NO_BOUNDARY) return fail(ctx->fail(WAVEY_E_LIMIT, "too many boundary nodes"));
+    sh.air_cells = (int64_t)air_n;
+    sh.n_boundary = (int64_t)grand[0];
+    sh.n_slots = (int64_t)grand[1];
+    if ((st = dalloc((void **)&g->bcell, 4 * (size_t)sh.n_boundary, true)) ||
+        (st = dalloc((void **)&g->bstart, 4 * ((size_t)sh.n_boundary + 1), true)) ||
+        (st = dalloc((void **)&g->slots, 32 * (size_t)sh.n_slots, true)))
+        return fail(st);
+    wk::grid_nodes<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_solid, g->flags, (uint32_t *)d_cnt, true,
+                                          (const uint32_t *)d_node_at, (const unsigned long long *)d_slot_at, g->bidx,
+                                          g->bcell, g->bstart, g->slots);
+    const uint32_t last = (uint32_t)sh.n_slots;
+    cudaMemcpyAsync(g->bstart + sh.n_boundary, &last, 4, cudaMemcpyHostToDevice, s);
+    if ((st = ctx->cuda(cudaStreamSynchronize(s), "grid build"))) return fail(st);
+    for (void *q : tmp) cudaFree(q);
+    g->shape = sh;
+    *shape = sh;
+    *out = g;
+    return WAVEY_OK;
+}
+
+int grid_read(wavey_device_grid *g, uint8_t *flags, uint32_t *bidx, uint32_t *bcell, uint32_t *bstart, double *slots) {
+    wavey_cuda_ctx *ctx = g->ctx;
+    const wavey_grid_shape &sh = g->shape;
+    const size_t cells = (size_t)sh.n[0] * sh.n[1] * sh.n[2];
+    if (!flags || !bidx || !bstart || (sh.n_boundary && !bcell) || (sh.n_slots && !slots))
+        return ctx->fail(WAVEY_E_INVALID, "null output array");
+    int st;
+    if ((st = ctx->cuda(cudaMemcpy(flags, g->flags, cells, cudaMemcpyDeviceToHost), "read flags")) ||
+        (st = ctx->cuda(cudaMemcpy(bidx, g->bidx, 4 * cells, cudaMemcpyDeviceToHost), "read bidx")) ||
+        (sh.n_boundary && (st = ctx->cuda(cudaMemcpy(bcell, g->bcell, 4 * (size_t)sh.n_boundary, cudaMemcpyDeviceToHost), "read bcell"))) ||
+        (st = ctx->cuda(cudaMemcpy(bstart, g->bstart, 4 * ((size_t)sh.n_boundary + 1), cudaMemcpyDeviceToHost), "read bstart")) ||
+        (sh.n_slots && (st = ctx->cuda(cudaMemcpy(slots, g->slots, 32 * (size_t)sh.n_slots, cudaMemcpyDeviceToHost), "read slots"))))
+        return st;
+    return WAVEY_OK;
+}
+
 int plan_read(wavey_cuda_plan *pl, double *out, double *ir_out) {
     wavey_cuda_ctx *ctx = pl->ctx;
     if (!pl->ran) return ctx->fail(WAVEY_E_INVALID, "the plan has not run");
@@ -1548,6 +1728,29 @@ int wavey_cuda_plan_band_params(wavey_cuda_plan *plan, const double *bands_hz, i
     std::lock_guard<std::mutex> lock(plan->ctx->mu);
     cudaSetDevice(plan->ctx->device);
     return plan_band_params(plan, bands_hz, n_bands, flags, out, out_doubles);
+}
+
+int wavey_cuda_grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int32_t n_fits, double c,
+                          double dx, wavey_device_grid **out, wavey_grid_shape *shape) {
+    if (!ctx) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return grid_build(ctx, room, fits, n_fits, c, dx, out, shape);
+}
+
+int wavey_cuda_grid_read(wavey_device_grid *grid, uint8_t *flags, uint32_t *bidx, uint32_t *bcell, uint32_t *bstart,
+                         double *slots) {
+    if (!grid) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(grid->ctx->mu);
+    cudaSetDevice(grid->ctx->device);
+    return grid_read(grid, flags, bidx, bcell, bstart, slots);
+}
+
+void wavey_cuda_grid_free(wavey_device_grid *grid) {
+    if (!grid) return;
+    std::lock_guard<std::mutex> lock(grid->ctx->mu);
+    cudaSetDevice(grid->ctx->device);
+    free_device_grid(grid);
 }
 
 int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
