@@ -599,7 +599,8 @@ int build_graph(wavey_cuda_plan *pl) {
             if (cudaGraphNodeGetType(n, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) pl->graph_kernels++;
         }
     }
-    e = cudaGraphInstantiate(&pl->graph, g, 0);
+    // Node priorities (the branch's launch attribute) count only with this flag.
+    e = cudaGraphInstantiateWithFlags(&pl->graph, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     return ctx->cuda(e, "graph instantiate");
 }
@@ -1471,7 +1472,7 @@ int rooms_graph(wavey_cuda_rooms *rm) {
         cudaGraphNodeType ty;
         if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) rm->graph_kernels++;
     }
-    e = cudaGraphInstantiate(&rm->graph, g, 0);
+    e = cudaGraphInstantiateWithFlags(&rm->graph, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     return ctx->cuda(e, "graph instantiate");
 }
