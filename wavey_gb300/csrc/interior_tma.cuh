@@ -174,6 +174,7 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
     // n+1 for the stores and their range limits -- staged once, so no plane
     // waits on them.
     float *ssc = reinterpret_cast<float *>(base + NP * PS + NQ * QB + 256);
+    unsigned int *wmax = reinterpret_cast<unsigned int *>(bars + 16);  // FP16: [2][8] warp maxima of two planes
     if constexpr (HALF) {
         const long long n = *a.base + a.t;
         const float2 *s_now = a.scale + ((int)(n % SCALE_RING) * a.chunks + c) * a.nz;
@@ -330,12 +331,11 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
         }
         if constexpr (HALF) {
             // A value beyond the FP16 range of its slab scale is an error,
-            // not a saturation; the warp's maximum raises the slab maximum by
-            // a reduction without return (RED).
+            // not a saturation.
             if (mb > __float_as_uint(slim) && *reinterpret_cast<volatile int *>(a.error) == 0)
                 atomicExch(a.error, ERR_FP16_RANGE);
             mb = __reduce_max_sync(0xffffffffu, mb);
-            if (lane == 0 && mb > 0u) atomicMax(amax_new + z, mb);
+            if (lane == 0) wmax[(j & 1) * 8 + warp] = mb;
             scm = scc;
             scc = scp;
         }
@@ -345,6 +345,15 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
             failed = true;
             if (threadIdx.x == 0) atomicExch(a.error, ERR_TMA_WAIT);
             break;
+        }
+        if constexpr (HALF) {
+            // The CTA's maximum of the plane raises the slab maximum with one
+            // reduction (RED): one per CTA and plane, not one per warp.
+            if (threadIdx.x == 0) {
+                unsigned int m = 0u;
+                for (int w = 0; w < 8; w++) m = max(m, wmax[(j & 1) * 8 + w]);
+                if (m > 0u) atomicMax(amax_new + z, m);
+            }
         }
         bm = bc;
         bc = bp;
