@@ -11,15 +11,13 @@
 //                  surface behind each missing face within 1.5 dx (fdtd.rs:357-363)
 //                  and boundary_slots (fdtd.rs:539-571); with `write`, its node
 //                  index, cell, first slot and slot constants
-//   scan_*         exclusive scan of the per-cell node and slot counts
+//   scan_*         exclusive scan of the per-cell node and slot counts, and the air count
 #pragma once
 #include <cstdint>
 
 #include "../../include/wavey_host.h"
 
 namespace wk {
-
-constexpr int GB_MAX_RECTS = 512;  // 6 + 4 pillars + 6 blocks per surface list
 
 struct GbRect {
     int axis;
@@ -76,22 +74,16 @@ __global__ void __launch_bounds__(256) grid_classify(GbRoom r, uint8_t *solid, u
     air[i] = !s && x > 0 && y > 0 && z > 0 && x < r.nx - 1 && y < r.ny - 1 && z < r.nz - 1 && gb_room_contains(r, p);
 }
 
-__global__ void __launch_bounds__(256) grid_flags(GbRoom r, const uint8_t *air, uint8_t *flags,
-                                                   unsigned long long *air_count) {
+__global__ void __launch_bounds__(256) grid_flags(GbRoom r, const uint8_t *air, uint8_t *flags) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long cells = r.nx * r.ny * r.nz;
-    unsigned a = 0;
-    if (i < cells && air[i]) {
-        const long long nxy = r.nx * r.ny;
-        const long long off[6] = {-1, 1, -r.nx, r.nx, -nxy, nxy};
-        uint8_t fl = WAVEY_AIR;
-        for (int k = 0; k < 6; k++)
-            if (air[i + off[k]]) fl |= (uint8_t)(1u << k);  // air cells are interior: i + off stays in the grid
-        flags[i] = fl;
-        a = 1;
-    }
-    a = __reduce_add_sync(0xffffffffu, a);
-    if ((threadIdx.x & 31) == 0 && a) atomicAdd(air_count, (unsigned long long)a);
+    if (i >= cells || !air[i]) return;
+    const long long nxy = r.nx * r.ny;
+    const long long off[6] = {-1, 1, -r.nx, r.nx, -nxy, nxy};
+    uint8_t fl = WAVEY_AIR;
+    for (int k = 0; k < 6; k++)
+        if (air[i + off[k]]) fl |= (uint8_t)(1u << k);  // air cells are interior: i + off stays in the grid
+    flags[i] = fl;
 }
 
 __device__ bool gb_fits_equal(const wh_fit &a, const wh_fit &b) {
@@ -221,59 +213,69 @@ __global__ void __launch_bounds__(256) grid_nodes(GbRoom r, const uint8_t *solid
 // per-block totals, a scan of the totals, then each block's own scan.
 constexpr int SCAN_BLOCK = 1024;
 
-__global__ void __launch_bounds__(SCAN_BLOCK) scan_totals(const uint32_t *cnt, long long n,
-                                                          unsigned long long *node_tot, unsigned long long *slot_tot) {
-    __shared__ unsigned long long sn[SCAN_BLOCK / 32], ss[SCAN_BLOCK / 32];
+__global__ void __launch_bounds__(SCAN_BLOCK) scan_totals(const uint32_t *cnt, const uint8_t *flags, long long n,
+                                                          unsigned long long *node_tot, unsigned long long *slot_tot,
+                                                          unsigned long long *air_tot) {
+    __shared__ unsigned long long sn[SCAN_BLOCK / 32], ss[SCAN_BLOCK / 32], sa[SCAN_BLOCK / 32];
     const long long i = (long long)blockIdx.x * SCAN_BLOCK + threadIdx.x;
     const uint32_t c = i < n ? cnt[i] : 0u;
-    unsigned long long a = c > 0 ? 1 : 0, b = c;
+    unsigned long long a = c > 0 ? 1 : 0, b = c, air = (i < n && (flags[i] & WAVEY_AIR)) ? 1 : 0;
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, o);
         b += __shfl_down_sync(0xffffffffu, b, o);
+        air += __shfl_down_sync(0xffffffffu, air, o);
     }
     if ((threadIdx.x & 31) == 0) {
         sn[threadIdx.x / 32] = a;
         ss[threadIdx.x / 32] = b;
+        sa[threadIdx.x / 32] = air;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long ta = 0, tb = 0;
+        unsigned long long ta = 0, tb = 0, tc = 0;
         for (int w = 0; w < SCAN_BLOCK / 32; w++) {
             ta += sn[w];
             tb += ss[w];
+            tc += sa[w];
         }
         node_tot[blockIdx.x] = ta;
         slot_tot[blockIdx.x] = tb;
+        air_tot[blockIdx.x] = tc;
     }
 }
 
 // One block: exclusive scan of the block totals in place (sequential chunks
 // per thread, then a scan of the chunk sums); also writes the grand totals.
 __global__ void __launch_bounds__(SCAN_BLOCK) scan_block_totals(unsigned long long *node_tot,
-                                                                unsigned long long *slot_tot, long long nb,
+                                                                unsigned long long *slot_tot,
+                                                                const unsigned long long *air_tot, long long nb,
                                                                 unsigned long long *grand) {
-    __shared__ unsigned long long cn[SCAN_BLOCK], cs[SCAN_BLOCK];
+    __shared__ unsigned long long cn[SCAN_BLOCK], cs[SCAN_BLOCK], ca[SCAN_BLOCK];
     const long long per = (nb + SCAN_BLOCK - 1) / SCAN_BLOCK;
     const long long a0 = (long long)threadIdx.x * per, a1 = min(a0 + per, nb);
-    unsigned long long sa = 0, sb = 0;
+    unsigned long long sa = 0, sb = 0, sc = 0;
     for (long long k = a0; k < a1; k++) {
         sa += node_tot[k];
         sb += slot_tot[k];
+        sc += air_tot[k];
     }
     cn[threadIdx.x] = sa;
     cs[threadIdx.x] = sb;
+    ca[threadIdx.x] = sc;
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned long long ra = 0, rb = 0;
+        unsigned long long ra = 0, rb = 0, rc = 0;
         for (int t = 0; t < SCAN_BLOCK; t++) {
             const unsigned long long va = cn[t], vb = cs[t];
             cn[t] = ra;
             cs[t] = rb;
             ra += va;
             rb += vb;
+            rc += ca[t];
         }
         grand[0] = ra;
         grand[1] = rb;
+        grand[2] = rc;
     }
     __syncthreads();
     unsigned long long ra = cn[threadIdx.x], rb = cs[threadIdx.x];

@@ -1295,7 +1295,7 @@ int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int
     };
     const long long nscan = (cells + wk::SCAN_BLOCK - 1) / wk::SCAN_BLOCK;
     void *d_pill = nullptr, *d_blk = nullptr, *d_sol = nullptr, *d_rects = nullptr, *d_fits = nullptr, *d_solid = nullptr,
-         *d_air = nullptr, *d_cnt = nullptr, *d_air_n = nullptr, *d_ntot = nullptr, *d_stot = nullptr, *d_grand = nullptr,
+         *d_air = nullptr, *d_cnt = nullptr, *d_atot = nullptr, *d_ntot = nullptr, *d_stot = nullptr, *d_grand = nullptr,
          *d_node_at = nullptr, *d_slot_at = nullptr;
     int st;
     if ((st = dalloc(&d_pill, sizeof(double) * 4 * room->n_pillars, false)) ||
@@ -1304,8 +1304,8 @@ int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int
         (st = dalloc(&d_rects, sizeof(wk::GbRect) * rects.size(), false)) ||
         (st = dalloc(&d_fits, sizeof(wh_fit) * n_fits, false)) || (st = dalloc(&d_solid, cells, false)) ||
         (st = dalloc(&d_air, cells, false)) || (st = dalloc(&d_cnt, 4 * (size_t)cells, false)) ||
-        (st = dalloc(&d_air_n, 8, false)) || (st = dalloc(&d_ntot, 8 * (size_t)nscan, false)) ||
-        (st = dalloc(&d_stot, 8 * (size_t)nscan, false)) || (st = dalloc(&d_grand, 16, false)) ||
+        (st = dalloc(&d_atot, 8 * (size_t)nscan, false)) || (st = dalloc(&d_ntot, 8 * (size_t)nscan, false)) ||
+        (st = dalloc(&d_stot, 8 * (size_t)nscan, false)) || (st = dalloc(&d_grand, 24, false)) ||
         (st = dalloc(&d_node_at, 4 * (size_t)cells, false)) || (st = dalloc(&d_slot_at, 8 * (size_t)cells, false)) ||
         (st = dalloc((void **)&g->flags, cells, true)) || (st = dalloc((void **)&g->bidx, 4 * (size_t)cells, true)))
         return fail(st);
@@ -1316,7 +1316,6 @@ int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int
     cudaMemcpyAsync(d_fits, fits, sizeof(wh_fit) * n_fits, cudaMemcpyHostToDevice, s);
     cudaMemsetAsync(g->flags, 0, cells, s);
     cudaMemsetAsync(g->bidx, 0xFF, 4 * (size_t)cells, s);
-    cudaMemsetAsync(d_air_n, 0, 8, s);
     wk::GbRoom r;
     r.x0 = room->x0, r.y0 = room->y0, r.x1 = room->x1, r.y1 = room->y1, r.height = room->height;
     r.n_pillars = room->n_pillars, r.n_blocks = room->n_blocks, r.n_solids = room->n_solids;
@@ -1329,23 +1328,24 @@ int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int
     r.dx = sh.dx, r.dt = sh.dt;
     const unsigned blocks = (unsigned)((cells + 255) / 256);
     wk::grid_classify<<<blocks, 256, 0, s>>>(r, (uint8_t *)d_solid, (uint8_t *)d_air);
-    wk::grid_flags<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_air, g->flags, (unsigned long long *)d_air_n);
+    wk::grid_flags<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_air, g->flags);
     wk::grid_nodes<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_solid, g->flags, (uint32_t *)d_cnt, false, nullptr,
                                           nullptr, nullptr, nullptr, nullptr, nullptr);
-    wk::scan_totals<<<(unsigned)nscan, wk::SCAN_BLOCK, 0, s>>>((const uint32_t *)d_cnt, cells,
-                                                               (unsigned long long *)d_ntot, (unsigned long long *)d_stot);
-    wk::scan_block_totals<<<1, wk::SCAN_BLOCK, 0, s>>>((unsigned long long *)d_ntot, (unsigned long long *)d_stot, nscan,
+    wk::scan_totals<<<(unsigned)nscan, wk::SCAN_BLOCK, 0, s>>>((const uint32_t *)d_cnt, g->flags, cells,
+                                                               (unsigned long long *)d_ntot, (unsigned long long *)d_stot,
+                                                               (unsigned long long *)d_atot);
+    wk::scan_block_totals<<<1, wk::SCAN_BLOCK, 0, s>>>((unsigned long long *)d_ntot, (unsigned long long *)d_stot,
+                                                       (const unsigned long long *)d_atot, nscan,
                                                        (unsigned long long *)d_grand);
     wk::scan_apply<<<(unsigned)nscan, wk::SCAN_BLOCK, 0, s>>>((const uint32_t *)d_cnt, cells,
                                                               (const unsigned long long *)d_ntot,
                                                               (const unsigned long long *)d_stot, (uint32_t *)d_node_at,
                                                               (unsigned long long *)d_slot_at);
-    unsigned long long grand[2] = {0, 0}, air_n = 0;
-    cudaMemcpyAsync(grand, d_grand, 16, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&air_n, d_air_n, 8, cudaMemcpyDeviceToHost, s);
+    unsigned long long grand[3] = {0, 0, 0};
+    cudaMemcpyAsync(grand, d_grand, 24, cudaMemcpyDeviceToHost, s);
     if ((st = ctx->cuda(cudaStreamSynchronize(s), "grid build"))) return fail(st);
     if (grand[0] >= (unsigned long long)WAVEY_NO_BOUNDARY) return fail(ctx->fail(WAVEY_E_LIMIT, "too many boundary nodes"));
-    sh.air_cells = (int64_t)air_n;
+    sh.air_cells = (int64_t)grand[2];
     sh.n_boundary = (int64_t)grand[0];
     sh.n_slots = (int64_t)grand[1];
     if ((st = dalloc((void **)&g->bcell, 4 * (size_t)sh.n_boundary, true)) ||
