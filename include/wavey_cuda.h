@@ -93,7 +93,8 @@ typedef struct {
     int32_t interior_kernel;              /* 1: TMA-fed z-march beside the special-cell kernel; 0: fused step kernel */
     int32_t tma_zt;                       /* z planes per CTA of the TMA kernel */
     int32_t tma_depth;                    /* shape of the TMA kernel, rows/p ring/old ring: 0: 8/6/4, 1: 8/8/4,
-                                             2: 16/6/4, 3: 16/8/4, 4: 16/5/3 (-1: no TMA kernel) */
+                                             2: 16/6/4, 3: 16/8/4, 4: 16/5/3, 5: 32/5/3, 6: 32/4/2
+                                             (-1: no TMA kernel) */
     int32_t branch;                       /* form of the special-cell branch beside it (see wavey_tune_result) */
 } wavey_plan_info;
 
@@ -201,7 +202,7 @@ int wavey_cuda_grid_read(wavey_device_grid *grid, uint8_t *flags, uint32_t *bidx
 void wavey_cuda_grid_free(wavey_device_grid *grid);
 
 /* Autotuner of a plan's step kernels (FP32 plans of at least 256 steps).
- * Stage 1 times every shape of the interior kernel -- tile rows (8 or 16)
+ * Stage 1 times every shape of the interior kernel -- tile rows (8, 16 or 32)
  * with ring depths, and z planes per CTA (8, 16, 32 and the runs that fill
  * one to four whole waves of resident CTAs); stage 2 times, with that shape,
  * every form of the concurrent special-cell branch -- its register cap

@@ -300,8 +300,8 @@ void launch_step(wavey_cuda_plan *pl, int t, int parity) {
 struct TmaCfg {
     int rows, np, nq;
 };
-constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4}, {8, 8, 4}, {16, 6, 4}, {16, 8, 4}, {16, 5, 3}};
-constexpr int TMA_NCFG = 5;
+constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4}, {8, 8, 4}, {16, 6, 4}, {16, 8, 4}, {16, 5, 3}, {32, 5, 3}, {32, 4, 2}};
+constexpr int TMA_NCFG = 7;
 
 template <class E, int V, int R, int NP, int NQ>
 void launch_tma(int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
@@ -327,6 +327,8 @@ void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, int prio, const CUtenso
         case 2: launch_tma<E, V, 16, 6, 4>(blocks, s, prio, p, q, ta); break;
         case 3: launch_tma<E, V, 16, 8, 4>(blocks, s, prio, p, q, ta); break;
         case 4: launch_tma<E, V, 16, 5, 3>(blocks, s, prio, p, q, ta); break;
+        case 5: launch_tma<E, V, 32, 5, 3>(blocks, s, prio, p, q, ta); break;
+        case 6: launch_tma<E, V, 32, 4, 2>(blocks, s, prio, p, q, ta); break;
         default: launch_tma<E, V, 8, 6, 4>(blocks, s, prio, p, q, ta); break;
     }
 }
@@ -340,7 +342,8 @@ cudaError_t tma_attr() {
 template <class E, int V>
 cudaError_t tma_attrs() {
     cudaError_t e[] = {tma_attr<E, V, 8, 6, 4>(), tma_attr<E, V, 8, 8, 4>(), tma_attr<E, V, 16, 6, 4>(),
-                       tma_attr<E, V, 16, 8, 4>(), tma_attr<E, V, 16, 5, 3>()};
+                       tma_attr<E, V, 16, 8, 4>(), tma_attr<E, V, 16, 5, 3>(), tma_attr<E, V, 32, 5, 3>(),
+                       tma_attr<E, V, 32, 4, 2>()};
     for (cudaError_t x : e)
         if (x != cudaSuccess) return x;
     return cudaSuccess;
@@ -673,6 +676,8 @@ int tma_occupancy(int cfg) {
         case 2: f = (const void *)wk::interior_tma<E, V, 16, 6, 4>, smem = wk::tma_smem_of<E, 16, 6, 4>(); break;
         case 3: f = (const void *)wk::interior_tma<E, V, 16, 8, 4>, smem = wk::tma_smem_of<E, 16, 8, 4>(); break;
         case 4: f = (const void *)wk::interior_tma<E, V, 16, 5, 3>, smem = wk::tma_smem_of<E, 16, 5, 3>(); break;
+        case 5: f = (const void *)wk::interior_tma<E, V, 32, 5, 3>, smem = wk::tma_smem_of<E, 32, 5, 3>(); break;
+        case 6: f = (const void *)wk::interior_tma<E, V, 32, 4, 2>, smem = wk::tma_smem_of<E, 32, 4, 2>(); break;
         default: f = (const void *)wk::interior_tma<E, V, 8, 6, 4>, smem = wk::tma_smem_of<E, 8, 6, 4>(); break;
     }
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, 256, smem) != cudaSuccess) {
@@ -968,14 +973,15 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if ((st = ctx->cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event create"))) return bail(st);
     if ((st = alloc(pl, &pl->err, sizeof(int)))) return bail(st);
     if (standalone && (precision == WAVEY_FP32 || precision == WAVEY_FP16_STORAGE) && tma_selected()) {
-        // Untuned default: 16-row tiles with 5/3-plane rings, the z-run that
-        // fills one wave of resident CTAs, and a special-cell branch capped at
-        // three blocks per SM -- the shape the autotuner most often picks.
+        // Untuned default: 16-row tiles with 5/3-plane rings (FP32) or 32-row
+        // tiles with 4/2-plane rings (FP16), the z-run that fills one wave of
+        // resident CTAs, and a special-cell branch capped at three blocks per
+        // SM -- the shapes the autotuner most often picks.
         cudaError_t e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 1>() : tma_attrs<float, 1>();
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 2>() : tma_attrs<float, 2>();
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 4>() : tma_attrs<float, 4>();
         if ((st = ctx->cuda(e, "shared memory attribute"))) return bail(st);
-        const int cfg = env_int("WAVEY_TMA_CFG", 4, 0, TMA_NCFG - 1);
+        const int cfg = env_int("WAVEY_TMA_CFG", precision == WAVEY_FP16_STORAGE ? 6 : 4, 0, TMA_NCFG - 1);
         const int zw = wave_zt(pl, cfg, 1);
         const int zt1 = zw ? std::max(8, zw) : 16;
         if ((st = tma_shape(pl, cfg, env_int("WAVEY_TMA_ZT", zt1, 1, 4096)))) return bail(st);
