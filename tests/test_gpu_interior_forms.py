@@ -46,3 +46,33 @@ def test_fp16_plan_uses_tma(backend):
     plan = backend.plan(g, [taps], sig[:300], rcv, freqs, precision=FP16_STORAGE)
     assert plan.info()["interior_kernel"] == 1
     plan.close()
+
+
+@pytest.mark.parametrize("precision", [FP32, FP16_STORAGE], ids=["fp32", "fp16"])
+@pytest.mark.parametrize("cfg", range(7))
+def test_every_tma_shape_agrees(backend, library, precision, cfg):
+    """Every tile shape of the TMA kernel (8, 16 or 32 rows with their ring
+    depths), with z-runs of 1 plane (a CTA per plane), 3 planes and 64
+    planes (longer than the grid: one run per tile column), gives the
+    register-queue kernel's results bit for bit."""
+    g, taps, sig, rcv, freqs = branch_room(library, 0.1)
+    comps = directional_components(g, (1.6, 1.3, 1.1))
+    sources = comps + [taps]
+    os.environ["WAVEY_INTERIOR"] = "regq"
+    try:
+        ref = backend.run_batch(g, sources, sig, rcv, freqs, precision=precision, ir=True)
+    finally:
+        del os.environ["WAVEY_INTERIOR"]
+    for zt in (1, 3, 64):
+        os.environ["WAVEY_TMA_CFG"], os.environ["WAVEY_TMA_ZT"] = str(cfg), str(zt)
+        try:
+            plan = backend.plan(g, sources, sig, rcv, freqs, precision=precision, ir=True)
+            info = plan.info()
+            assert (info["tma_depth"], info["tma_zt"]) == (cfg, zt)
+            plan.run()
+            spec, ir = plan.read()
+            plan.close()
+        finally:
+            del os.environ["WAVEY_TMA_CFG"], os.environ["WAVEY_TMA_ZT"]
+        assert np.array_equal(ir, ref[1]), (cfg, zt)
+        assert np.array_equal(spec, ref[0]), (cfg, zt)
