@@ -116,6 +116,17 @@ __device__ __forceinline__ void ld4(const __half *p, float o[4], float sc) {
     o[3] = __high2float(b) * sc;
 }
 
+// The same without the slab scale: FP16 values as stored, converted exactly.
+__device__ __forceinline__ void ld4u(const float *p, float o[4]) { ld4(p, o, 1.0f); }
+__device__ __forceinline__ void ld4u(const __half *p, float o[4]) {
+    const uint2 raw = *reinterpret_cast<const uint2 *>(p);
+    const __half2 a = *reinterpret_cast<const __half2 *>(&raw.x), b = *reinterpret_cast<const __half2 *>(&raw.y);
+    o[0] = __low2float(a);
+    o[1] = __high2float(a);
+    o[2] = __low2float(b);
+    o[3] = __high2float(b);
+}
+
 // V: sources per cell in a chunk (1, 2 or 4); a tile row holds 128 / V cells.
 // R: rows per tile (8 or 16; 256 threads, R / 8 rows per thread).
 // NP / NQ: planes in the two rings; NP - 3 p planes and NQ - 1 old planes are
@@ -279,23 +290,31 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
                 if (!bits) continue;
                 const int row = warp + 8 * r;
                 const E *rc = pc + (row + 1) * PROW;
+                // The plane's own values (x and y neighbours, centre) are read
+                // without the slab scale: it is a power of two, so the first
+                // three sums scaled once give the scaled sums bit for bit (FP16
+                // values scaled stay far inside FP32's normal range).
                 float w[12], vym[4], vyp[4], vod[4];
-                ld4(rc + g - 4, w, scc);
-                ld4(rc + g + 4, w + 8, scc);
-                ld4(rc + g, w + 4, scc);
+                ld4u(rc + g - 4, w);
+                ld4u(rc + g + 4, w + 8);
+                ld4u(rc + g, w + 4);
                 float zmv[4], zpv[4];
                 ld4(pm + (row + 1) * PROW + g, zmv, scm);
                 ld4(pn + (row + 1) * PROW + g, zpv, scp);
-                ld4(pc + row * PROW + g, vym, scc);
-                ld4(pc + (row + 2) * PROW + g, vyp, scc);
+                ld4u(pc + row * PROW + g, vym);
+                ld4u(pc + (row + 2) * PROW + g, vyp);
                 ld4(qo + row * TMA_ROW_FLOATS + lane * 4, vod, sco);
                 float nx4[4];
 #pragma unroll
                 for (int e = 0; e < 4; e++) {
-                    const float cv = w[4 + e];
+                    float cv = w[4 + e];
                     float s = radd(w[4 + e - V], w[4 + e + V]);
                     s = radd(s, vym[e]);
                     s = radd(s, vyp[e]);
+                    if constexpr (HALF) {
+                        cv = rmul(cv, scc);
+                        s = rmul(s, scc);
+                    }
                     s = radd(s, zmv[e]);
                     s = radd(s, zpv[e]);
                     nx4[e] = radd(rsub(rmul(2.0f, cv), vod[e]), rmul(a.l2, rsub(s, rmul(6.0f, cv))));
