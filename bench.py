@@ -21,6 +21,11 @@ right-hand sides, batched in one launch per time step, FP32.  The fields
             span measured with CUDA events around each chunk's step launches
   plain     the same four right-hand sides run one at a time (S = 1 kernel)
 
+Other workloads: room_hall (the 376 M-cell hall, 64 right-hand sides, a bounded prefix of its steps) and
+room_pillars_32spk (the mixed-precision configuration: the pillar room with 32 seeded speakers = 71
+right-hand sides; with --precision fp16 --ir-accuracy it reports the FP16-storage throughput and the error
+of every mic impulse response and octave-band level against an FP64 GPU run of the same grid).
+
 --impl reference times the reference's CPU algorithm (the oracle's C
 restatement of fdtd::run_cpu, FP64, OpenMP over z-slabs as the reference's
 rayon loop) on the host cores, on a bounded sample of the same workload.
@@ -164,6 +169,10 @@ def make_scene(workload: str, seed: int, args=None):
         return W.room_pillars(seed=2)
     if workload == "room_small":
         return W.room_small(seed=1)
+    if workload == "room_pillars_32spk":
+        # The mixed-precision configuration: room_pillars' room with 32 seeded
+        # speakers (monopoles and cardioids), run with --precision fp16.
+        return W.room_pillars_speakers(32)
     if workload == "room_hall":
         # 376 M cells: a full 2 s run is 34,641 steps; the throughput of a step
         # does not change along the run, so a bounded prefix is timed.
@@ -356,6 +365,47 @@ def run_ours(args, rank, world):
                "spectra_worst_rel": float(np.abs(spec32 - spec64).max() / np.abs(spec64).max()),
                "reference": "FP64 GPU run of the same grid (WAVEY_FP64)"}
 
+    # Receiver impulse responses against an FP64 GPU run of the same grid
+    # (the mixed-precision configuration): every right-hand side at every mic,
+    # IR mode, and octave-band levels of the mics' spectra.
+    ir_acc = None
+    if args.ir_accuracy:
+        mics = scene.receivers[:scene.notes.get("mics", len(scene.receivers))]
+        out = {}
+        for prec in (main_precision, FP64):
+            pi = b.plan(g, scene.sources, scene.signal, mics, scene.freqs, prec, ir=True)
+            pi.run()
+            out[prec] = pi.read()
+            pi.close()
+        (spec_m, ir_m), (spec_d, ir_d) = out[main_precision], out[FP64]
+        ir_peak = np.abs(ir_d).max(axis=-1)                   # [S][mics]
+        rel = np.abs(ir_m - ir_d).max(axis=-1) / np.where(ir_peak > 0, ir_peak, 1.0)
+        h0 = np.ones(len(scene.freqs), complex)
+        tm = np.stack([to_transfer(spec_m[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
+        td = np.stack([to_transfer(spec_d[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
+        cent = [c for c in W.OCTAVES if c <= scene.crossover]
+
+        def band_err(a, b):
+            d = np.abs(W.octave_levels(a, scene.freqs, cent) - W.octave_levels(b, scene.freqs, cent))
+            return {"worst": float(d.max()), "p99": float(np.quantile(d, 0.99)), "median": float(np.median(d)),
+                    "per_band_worst": [float(x) for x in d.reshape(-1, len(cent)).max(axis=0)]}
+
+        ir_acc = {"precision": args.precision, "reference": "FP64 GPU run of the same grid (WAVEY_FP64)",
+                  "impulse_responses": int(rel.size), "mics": len(mics), "right_hand_sides": S,
+                  "ir_max_abs_err_over_peak": {"worst": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+                                               "median": float(np.median(rel))},
+                  "octave_bands_hz": cent,
+                  "octave_band_abs_db_per_rhs": band_err(tm, td)}
+        if scene.notes.get("speaker_rhs"):
+            # Each speaker's transfer function: its right-hand sides combined
+            # with its component weights (a monopole's is its one RHS).
+            def speakers(t):
+                return np.stack([np.einsum("fc,crf->rf", np.array(w), t[a:a + n])
+                                 for (a, n), w in zip(scene.notes["speaker_rhs"], scene.notes["speaker_weights"])])
+            ir_acc["speakers"] = len(scene.notes["speaker_rhs"])
+            ir_acc["octave_band_abs_db_per_speaker"] = band_err(speakers(tm), speakers(td))
+        log(f"[rank {rank}] IR accuracy vs FP64: {ir_acc}")
+
     # FP16 field storage: throughput and its error against the FP64 run.
     fp16 = None
     if not args.no_fp16:
@@ -425,6 +475,7 @@ def run_ours(args, rank, world):
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": info["h2d_bytes"],
                     "d2h_bytes_per_step": info["d2h_bytes"], "seconds": e2e_s},
             "accuracy": acc,
+            "ir_accuracy": ir_acc,
             "fp16_storage": fp16,
             "grid_build": grid_build,
             "cpu_baseline": cpu,
@@ -454,6 +505,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--hall-steps", type=int, default=384)
     ap.add_argument("--hall-speakers", type=int, default=16)
+    ap.add_argument("--ir-accuracy", action="store_true",
+                    help="impulse responses of every right-hand side at the mics and their octave-band levels "
+                         "against an FP64 GPU run (IR mode)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warm-up raised to 3 (timing rule)")

@@ -154,25 +154,38 @@ def room_pillars(seed: int = 2, duration: float = 1.0, n_materials: int = 5, pla
 
 def room_pillars_speakers(n_speakers: int, seed: int = 4, duration: float = 1.0) -> Scene:
     """room_pillars' room and materials with n seeded speakers; each speaker
-    is a monopole or a cardioid (4 right-hand sides)."""
+    is a monopole or a cardioid (4 right-hand sides) at a seeded yaw and
+    pitch.  notes["speaker_rhs"] holds each speaker's (first right-hand side,
+    count) and notes["speaker_weights"] its per-frequency component weights
+    ([nf][count]; 1 for a monopole), which combine its right-hand sides into
+    the speaker's transfer function as the reference's wave stage does
+    (run.rs:626-660)."""
     base = room_pillars(seed=2, duration=duration)
     rng = np.random.default_rng(seed)
     g = base.grid
-    sources = []
-    kinds = []
+    sources, kinds, rhs, weights = [], [], [], []
     for _ in range(n_speakers):
         pos = _random_points(rng, base.room, 1, margin=1.5)[0]
         node = g.nearest_air(pos)
+        first = len(sources)
         if rng.uniform() < 0.5:
             sources.append(g.taps_at(pos))
             kinds.append("monopole")
+            weights.append([[1.0 + 0.0j] for _f in base.freqs])
         else:
             sources.extend(source_components(g, node, 1))
             kinds.append("cardioid")
+            rot = speaker_rotation(float(rng.uniform(0, 360)), float(rng.uniform(-30, 30)), 0.0)
+            w = []
+            for f in base.freqs:
+                a0, a, _res = fit_first_order(cardioid, rot, f)
+                w.append(component_weights(a0, a, 2.0 * math.pi * f / C_AIR, g.dx))
+            weights.append(w)
+        rhs.append((first, len(sources) - first))
     base.name = f"room_pillars_{n_speakers}spk"
     base.sources = sources
     base.weights = []
-    base.notes = dict(base.notes, speakers=kinds)
+    base.notes = dict(base.notes, speakers=kinds, speaker_rhs=rhs, speaker_weights=weights)
     return base
 
 
