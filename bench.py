@@ -21,7 +21,9 @@ right-hand sides, batched in one launch per time step, FP32.  The fields
             span measured with CUDA events around each chunk's step launches
   plain     the same four right-hand sides run one at a time (S = 1 kernel)
 
-Other workloads: room_hall (the 376 M-cell hall, 64 right-hand sides, a bounded prefix of its steps) and
+Other workloads: room_hall (the 376 M-cell hall, 64 right-hand sides, a bounded prefix of its steps),
+rooms_batch (room_small's room with 32 speakers plus four shoeboxes in one launch per step, against every
+right-hand side run alone) and
 room_pillars_32spk (the mixed-precision configuration: the pillar room with 32 seeded speakers = 71
 right-hand sides; with --precision fp16 --ir-accuracy it reports the FP16-storage throughput and the error
 of every mic impulse response and octave-band level against an FP64 GPU run of the same grid).
@@ -228,6 +230,75 @@ def run_reference(args, rank, world):
                  "fdtd::run_cpu is timed through the oracle's C restatement on the host cores",
     }
     print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ many rooms
+def run_rooms(args, rank, world):
+    """The multi-room configuration (workload rooms_batch): room_small's room
+    with 32 speakers plus four shoeboxes, every room with its own right-hand
+    sides, signals and receivers, advanced together in one launch per time
+    step (wavey_cuda_rooms_*), against every right-hand side run alone."""
+    from wavey_gb300 import _build
+
+    _build.build()
+    import torch
+
+    from wavey_gb300 import workloads as W
+    from wavey_gb300.backend import FP32, CudaBackend, RoomJob
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    scenes = W.rooms_batch()
+    jobs = [RoomJob(sc.grid, sc.sources, sc.signal, sc.receivers, sc.freqs) for sc in scenes]
+    updates = sum(sc.grid.air * sc.steps * len(sc.sources) for sc in scenes)
+    rhs = sum(len(sc.sources) for sc in scenes)
+    b = CudaBackend(dev)
+    p = b.rooms_plan(jobs)
+    for _ in range(args.warmup):
+        p.run()
+    barrier(world)
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    with ClockSampler(dev) as clocks:
+        for _ in range(args.steps):
+            total_ms += p.run(stats=True)["total_ms"]
+    torch.cuda.synchronize()
+    barrier(world)
+    elapsed = max_over_ranks(total_ms / 1e3, world)
+    value = updates * args.steps * world / elapsed / 1e9
+    info = p.info(0)
+    steps = max(sc.steps for sc in scenes)
+    launches = info["graph_kernels"] * (steps // 128) + (steps % 128 + 2 if steps % 128 else 0)
+    p.close()
+    # Every right-hand side alone, one standalone plan each.
+    t_plain = 0.0
+    if not args.no_plain:
+        for sc in scenes:
+            for src in sc.sources:
+                q = b.plan(sc.grid, [src], sc.signal, sc.receivers, sc.freqs, FP32)
+                q.run()
+                t_plain += q.run(stats=True)["total_ms"] / 1e3
+                q.close()
+    plain = updates / t_plain / 1e9 if t_plain else None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "rooms_batch", "rooms": len(scenes), "right_hand_sides": rhs,
+                       "grids": [list(sc.grid.n) for sc in scenes], "time_steps": steps,
+                       "l2": "small grids (not HBM-bound); no flush",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+            "per_source": value / rhs,
+            "plain": {"value": plain, "batched_over_plain": None if plain is None else value / world / plain},
+            "roofline": None,
+            "e2e": None,
+            "cpu_baseline": None,
+            "gpu_launches": int(launches * args.steps),
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    b.close()
 
 
 # ------------------------------------------------------------------ our arm
@@ -515,6 +586,8 @@ def main():
     rank, world = dist_init()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "rooms_batch":
+        run_rooms(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:
