@@ -59,3 +59,26 @@ def test_reference_arm_runs_on_rank_zero_only():
     # Rank 1 returns at once with no output; rank 0's work is tested by the
     # bench itself.
     assert bench.run_reference(A(), 1, 2) is None
+
+
+def test_reference_arm_line(capsys):
+    """Rank 0 of the reference arm times the reference's CPU loop (the
+    oracle's restatement of run_cpu) on a bounded sample and prints one JSON
+    line with the contract's keys."""
+    import json
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    class A:
+        workload, warmup, steps, sample_steps = "room_small", 3, 2, 20
+
+    bench.run_reference(A(), 0, 1)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["value"] > 0 and line["higher_is_better"] is True and line["steps"] == 2 and line["warmup"] == 3
+    assert line["config"]["workload"] == "room_small"
+    cb = line["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and "20 of" in cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": bench.UNIT, "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
