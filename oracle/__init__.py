@@ -8,6 +8,11 @@ product (wavey_gb300) never imports it.
                  loop in FP32 in the reference shader's operation order
                  (fdtd.wgsl:44-119), compiled by build.py into
                  oracle/_build/libwavey_oracle.so
+  fp16_oracle.c  the FP32 loop with the fields stored as FP16 times a power of
+                 two per z slab and time level (the FP16-storage form of the
+                 CUDA path: slab scales, rounding, slab maxima)
+  ir_oracle.c    the IR post-processing (analysis.rs:143-325): octave
+                 band-pass, onset, Schroeder / Lundeby, ISO 3382-1 parameters
   voxel.py       numpy restatement of FdtdGrid::build_dx (fdtd.rs:289-378)
                  and boundary_slots (fdtd.rs:539-571) for box rooms
 

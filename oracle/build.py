@@ -14,7 +14,7 @@ OUT = HERE / "_build" / "libwavey_oracle.so"
 
 
 def build(force: bool = False) -> Path:
-    srcs = [HERE / "fdtd_oracle.c", HERE / "ir_oracle.c"]
+    srcs = [HERE / "fdtd_oracle.c", HERE / "fp16_oracle.c", HERE / "ir_oracle.c"]
     if not force and OUT.exists() and all(OUT.stat().st_mtime >= s.stat().st_mtime for s in srcs):
         return OUT
     OUT.parent.mkdir(exist_ok=True)
