@@ -205,10 +205,14 @@ void wavey_cuda_grid_free(wavey_device_grid *grid);
  * Stage 1 times every shape of the interior kernel -- tile rows (8, 16 or 32)
  * with ring depths, and z planes per CTA (8, 16, 32 and the runs that fill
  * one to four whole waves of resident CTAs); stage 2 times, with that shape,
- * every form of the concurrent special-cell branch -- its register cap
- * (branch / 3: 1, 3 or 4 blocks per SM) and launch priority (branch % 3:
- * equal, special cells first, interior first).  Each candidate runs two
- * 128-step chunks of the plan's own grid, and the plan keeps the fastest.
+ * every form of the special-cell update: forms 0-8 run it in a concurrent
+ * kernel, with its register cap (branch / 3: 1, 3 or 4 blocks per SM) and
+ * launch priority (branch % 3: equal, special cells first, interior first);
+ * form 9 (FP32 plans) has every interior CTA update the special cells of its
+ * own tile from the planes it stages, with only the receiver samples on the
+ * concurrent kernel.  If form 9 wins, stage 3 times every interior shape
+ * again with it.  Each candidate runs two 128-step chunks of the plan's own
+ * grid, and the plan keeps the fastest.
  * result (nullable) lists the candidates' step times.  Neither stage changes
  * any arithmetic.  Other plans are left as they are. */
 #define WAVEY_TUNE_MAX 64
@@ -270,9 +274,13 @@ void wavey_cuda_rooms_destroy(wavey_cuda_rooms *rooms);
  *
  * Scratch is one fixed 2 MiB array inside the library (every GPU that loads
  * the library holds it until exit).  The first call on a device looks up
- * that array's device address, so make it before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race and must be
- * serialised by the caller. */
+ * that array's device address, so make it before any stream capture; after
+ * a device reset (cudaDeviceReset) the next call looks it up again, so make
+ * that call before any capture too.  All calls share the array.  A call
+ * queues all of its kernels under one process-wide lock, so calls from
+ * several host threads on one stream do not interleave; calls on different
+ * streams whose kernels overlap on the GPU race and must be serialised by
+ * the caller. */
 #define WAVEY_NOALLOC_MAX_FREQS 2048
 int wavey_cuda_receiver_dft_noalloc(int device, const float *series, int64_t n_recv, int64_t steps, const double *freqs,
                                     int64_t nf, double dt, double *out, void *stream, char *err, size_t err_cap);

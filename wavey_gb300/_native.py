@@ -29,6 +29,9 @@ WAVEY_FP32 = 0
 WAVEY_FP64 = 1
 WAVEY_FP16_STORAGE = 2
 
+# include/wavey_cuda.h: frequency limit of wavey_cuda_receiver_dft_noalloc
+WAVEY_NOALLOC_MAX_FREQS = 2048
+
 WH_MAX_BRANCHES = 4
 WH_FIT_DIRECTIONS = 400
 
@@ -175,6 +178,19 @@ def host() -> C.CDLL:
         "wh_grid_build": (C.c_int, [C.POINTER(WhRoom), C.POINTER(WhFit), C.c_int32, C.c_double, C.c_double,
                                     C.POINTER(C.c_void_p)]),
         "wh_grid_spacing": (C.c_double, [C.POINTER(WhRoom), C.c_double, C.c_double, C.c_double]),
+        "wh_mesh_room_build": (C.c_int, [c_double_p, C.c_int64, c_uint32_p, c_int64_p, C.POINTER(C.c_int32),
+                                         C.c_int64, C.POINTER(C.c_void_p)]),
+        "wh_mesh_room_free": (None, [C.c_void_p]),
+        "wh_mesh_room_surface_count": (C.c_int32, [C.c_void_p]),
+        "wh_mesh_room_triangle_count": (C.c_int64, [C.c_void_p]),
+        "wh_mesh_room_surface": (None, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                        c_double_p, c_double_p, c_double_p]),
+        "wh_mesh_room_triangles": (None, [C.c_void_p, c_double_p, c_uint32_p]),
+        "wh_mesh_room_bounds": (None, [C.c_void_p, c_double_p, c_double_p]),
+        "wh_mesh_room_contains": (C.c_int, [C.c_void_p, c_double_p]),
+        "wh_mesh_room_volume": (C.c_double, [C.c_void_p]),
+        "wh_grid_build_mesh": (C.c_int, [C.c_void_p, c_double_p, C.c_int32, C.POINTER(WhFit), C.c_int32,
+                                         C.c_double, C.c_double, C.POINTER(C.c_void_p)]),
         "wh_grid_view_of": (None, [C.c_void_p, C.POINTER(WhGridView)]),
         "wh_grid_free": (None, [C.c_void_p]),
         "wh_grid_alloc": (C.c_int, [c_int64_p, c_double_p, C.c_double, C.c_double, C.c_int64, C.c_int64, C.c_int64,

@@ -18,15 +18,21 @@
 // first call on each device looks up its device address with
 // cudaGetSymbolAddress while that device is current, and passes that address
 // to the kernels.  That first call should therefore be made before any
-// stream capture begins.
+// stream capture begins.  The address is remembered together with the
+// device's current context; after a device reset (a new primary context, in
+// which the library's module is loaded again) the next call looks it up anew.
 //
 // Every call shares the one scratch array, and each call overwrites it
 // completely before reading it, so nothing in it needs clearing; the output
-// is cleared by the call itself.  Calls whose kernels overlap on the GPU
-// (for example on two different streams) race on the scratch and give wrong
-// results: serialise them.
+// is cleared by the call itself.  A call queues all of its work while holding
+// one process-wide lock, so calls from several host threads on the same
+// stream never interleave their kernels.  Calls whose kernels overlap on the
+// GPU (for example on two different streams) race on the scratch and give
+// wrong results: serialise them.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 
@@ -73,8 +79,31 @@ __global__ void na_accumulate(const float *series, long long steps, const float2
     out[2 * idx + 1] += (double)im;
 }
 
+// Per device: the scratch array's device address and the context it was
+// looked up in.
+struct ScratchAddr {
+    CUcontext ctx;
+    float2 *addr;
+};
 std::mutex g_mu;
-float2 *g_addr[NA_MAX_DEVICES] = {};
+ScratchAddr g_addr[NA_MAX_DEVICES] = {};
+
+// The calling thread's current context (cuCtxGetCurrent, fetched from the
+// driver once, so that the library needs no link-time libcuda).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+CUcontext current_context() {
+    static CtxGetCurrentFn fn = []() -> CtxGetCurrentFn {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            return reinterpret_cast<CtxGetCurrentFn>(p);
+        return nullptr;
+    }();
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
 
 void message(char *err, size_t cap, const char *text) {
     if (err && cap) snprintf(err, cap, "%s", text);
@@ -100,6 +129,10 @@ extern "C" int wavey_cuda_receiver_dft_noalloc(int device, const float *series, 
         message(err, err_cap, buf);
         return WAVEY_E_LIMIT;
     }
+    if (nf > 0 && n_recv > INT64_MAX / nf) {
+        message(err, err_cap, "too many receivers x frequencies for one launch");
+        return WAVEY_E_LIMIT;
+    }
     if (n_recv * nf == 0) return WAVEY_OK;
     if ((n_recv * nf + NA_BLOCK - 1) / NA_BLOCK >= (1ll << 31)) {
         message(err, err_cap, "too many receivers x frequencies for one launch");
@@ -115,33 +148,37 @@ extern "C" int wavey_cuda_receiver_dft_noalloc(int device, const float *series, 
         message(err, err_cap, "cannot make the device current");
         return WAVEY_E_CUDA;
     }
-    float2 *tw = nullptr;
+    cudaError_t e = cudaSuccess;
     {
+        // Held until the last launch is queued: calls from several host
+        // threads on one stream then queue their kernels one call after the
+        // other, and none reads another's twiddles.
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_addr[device]) {
+        ScratchAddr &slot = g_addr[device];
+        // cudaSetDevice above made the device's primary context current (it
+        // initialises it since CUDA 12), so this is the context the kernels
+        // run in.
+        const CUcontext ctx = current_context();
+        if (!slot.addr || !ctx || slot.ctx != ctx) {
             void *p = nullptr;
-            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
-            if (e != cudaSuccess || !p) {
-                cudaGetLastError();
-                cudaSetDevice(prev);
-                message(err, err_cap, cudaGetErrorString(e));
-                return WAVEY_E_CUDA;
-            }
-            g_addr[device] = static_cast<float2 *>(p);
+            e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
+            if (e == cudaSuccess && !p) e = cudaErrorInvalidSymbol;
+            if (e == cudaSuccess) slot = ScratchAddr{ctx, static_cast<float2 *>(p)};
         }
-        tw = g_addr[device];
+        float2 *const tw = slot.addr;
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, (size_t)(n_recv * nf) * 2 * sizeof(double), s);
+        for (int64_t n0 = 0; e == cudaSuccess && n0 < steps; n0 += NA_CHUNK) {
+            const int count = (int)((steps - n0) < NA_CHUNK ? (steps - n0) : NA_CHUNK);
+            const int tw_threads = count * (int)nf;
+            na_twiddles<<<(tw_threads + NA_BLOCK - 1) / NA_BLOCK, NA_BLOCK, 0, s>>>(tw, freqs, (int)nf, dt, n0, count);
+            const long long total = n_recv * nf;
+            na_accumulate<<<(unsigned)((total + NA_BLOCK - 1) / NA_BLOCK), NA_BLOCK, 0, s>>>(series, steps, tw, out,
+                                                                                             n_recv, (int)nf, n0, count);
+            e = cudaGetLastError();
+        }
     }
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    cudaError_t e = cudaMemsetAsync(out, 0, (size_t)(n_recv * nf) * 2 * sizeof(double), s);
-    for (int64_t n0 = 0; e == cudaSuccess && n0 < steps; n0 += NA_CHUNK) {
-        const int count = (int)((steps - n0) < NA_CHUNK ? (steps - n0) : NA_CHUNK);
-        const int tw_threads = count * (int)nf;
-        na_twiddles<<<(tw_threads + NA_BLOCK - 1) / NA_BLOCK, NA_BLOCK, 0, s>>>(tw, freqs, (int)nf, dt, n0, count);
-        const long long total = n_recv * nf;
-        na_accumulate<<<(unsigned)((total + NA_BLOCK - 1) / NA_BLOCK), NA_BLOCK, 0, s>>>(series, steps, tw, out, n_recv,
-                                                                                         (int)nf, n0, count);
-        e = cudaGetLastError();
-    }
+    if (e != cudaSuccess) cudaGetLastError();
     cudaSetDevice(prev);
     if (e != cudaSuccess) {
         message(err, err_cap, cudaGetErrorString(e));
