@@ -28,6 +28,7 @@ def lib() -> C.CDLL:
             f.restype = C.c_int
             f.argtypes = args
         L.wo_max_threads.restype = C.c_int
+        L.wo_last_loop_seconds.restype = C.c_double
         L.wo_run_f16.restype = C.c_int
         L.wo_run_f16.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_double, u8p, u32p, C.c_int64, u32p, dp,
                                  C.c_int64, i64p, i64p, dp, dp, C.c_int64, i64p, C.c_int64, dp, C.c_int]
@@ -37,6 +38,12 @@ def lib() -> C.CDLL:
 
 def max_threads() -> int:
     return lib().wo_max_threads()
+
+
+def last_loop_seconds() -> float:
+    """Seconds of the step loop of the last FP64 run, without its allocation
+    and first touch of the fields."""
+    return float(lib().wo_last_loop_seconds())
 
 
 def _p(a, t):

@@ -44,6 +44,7 @@
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -69,6 +70,22 @@ int wo_max_threads(void) {
     return 1;
 #endif
 }
+
+static double now_seconds(void) {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+#endif
+}
+
+/* Seconds spent in the time-step loop of the last wo_run_f64 call, after the
+ * fields were allocated and first touched (for timing the CPU baseline
+ * without its set-up). */
+static double g_last_loop_seconds = 0.0;
+double wo_last_loop_seconds(void) { return g_last_loop_seconds; }
 
 /* -------------------------------------------------------------------------
  * FP64: fdtd.rs:644-725
@@ -127,6 +144,14 @@ int wo_run_f64(int64_t nx, int64_t ny, int64_t nz, double dt,
         return -1;
     }
     memset(out, 0, sizeof(double) * 2 * (size_t)(n_recv * nf));
+    /* First touch of both fields by the threads that update them (the loop's
+     * static z-slab schedule), before the timed loop. */
+#pragma omp parallel for schedule(static)
+    for (int64_t z = 0; z < nz; z++) {
+        memset(p + (size_t)(z * sxy), 0, sizeof(double) * (size_t)sxy);
+        memset(prev + (size_t)(z * sxy), 0, sizeof(double) * (size_t)sxy);
+    }
+    const double t_loop = now_seconds();
     for (int64_t n = 0; n < steps; n++) {
         record64(p, recv, (size_t)n_recv, freqs, (size_t)nf, dt, (size_t)n, out, ir, (size_t)steps);
         /* fdtd.rs:699-708: z-slabs in parallel, plain air only. */
@@ -168,6 +193,7 @@ int wo_run_f64(int64_t nx, int64_t ny, int64_t nz, double dt,
         for (int64_t t = 0; t < n_taps; t++) prev[tap_cell[t]] += tap_w[t] * signal[n];
         double *tmp = p; p = prev; prev = tmp;
     }
+    g_last_loop_seconds = now_seconds() - t_loop;
     free(p); free(prev); free(st_u); free(st_g); free(bnext);
     return 0;
 }
