@@ -152,6 +152,37 @@ def room_pillars(seed: int = 2, duration: float = 1.0, n_materials: int = 5, pla
                         "mics": len(mics), "plane_points": len(plane)})
 
 
+def room_pillars_shard(rank: int, world: int, seed: int = 7) -> Scene:
+    """room_pillars split by source over `world` GPUs: one cardioid speaker
+    (four right-hand sides) per rank, on the same grid.  Speaker 0 is
+    room_pillars' own source, so one rank runs exactly room_pillars; speakers
+    1..world-1 are seeded cardioids at seeded yaw and pitch.  No rank needs
+    another's data: the only exchange is gathering the spectra afterwards."""
+    if not 0 <= rank < world:
+        raise ValueError("rank outside the world")
+    base = room_pillars(seed=2)
+    if rank == 0:
+        base.notes = dict(base.notes, shard=f"speaker 0 of {world}")
+        return base
+    rng = np.random.default_rng([seed, rank])
+    g = base.grid
+    while True:
+        pos = _random_points(rng, base.room, 1, margin=2.0)[0]
+        comps = source_components(g, g.nearest_air(pos), 1)
+        if comps is not None:
+            break
+    yaw, pitch = float(rng.uniform(0, 360)), float(rng.uniform(-30, 30))
+    rot = speaker_rotation(yaw, pitch, 0.0)
+    weights = []
+    for f in base.freqs:
+        a0, a, _res = fit_first_order(cardioid, rot, f)
+        weights.append(component_weights(a0, a, 2.0 * math.pi * f / C_AIR, g.dx))
+    base.sources = comps
+    base.weights = weights
+    base.notes = dict(base.notes, source=pos, yaw=yaw, pitch=pitch, shard=f"speaker {rank} of {world}")
+    return base
+
+
 def room_pillars_speakers(n_speakers: int, seed: int = 4, duration: float = 1.0) -> Scene:
     """room_pillars' room and materials with n seeded speakers; each speaker
     is a monopole or a cardioid (4 right-hand sides) at a seeded yaw and
