@@ -86,6 +86,36 @@ int32_t wh_room_surface_count(const wh_room *room);
 /* Strict inside test of the room (room.rs:151-157 for the prism part). */
 int wh_room_contains(const wh_room *room, const double p[3]);
 
+/* -------------------------------------------------------------- mesh rooms
+ * Rooms imported as polygon meshes (OBJ rooms), room_from_mesh
+ * (wavey-geom room.rs:399-461): polygons are cut into triangles, each
+ * (material group, plane) becomes one surface with its normal into the room
+ * (found by the ray-parity inside test, room.rs:355-367), and surfaces are
+ * numbered in discovery order.  A surface's material is its group's.
+ */
+typedef struct wh_mesh_room wh_mesh_room;
+
+/* verts: [n_verts][3]; polygon f is face_verts[face_start[f] ..
+ * face_start[f + 1]) with material group face_group[f]. */
+int wh_mesh_room_build(const double *verts, int64_t n_verts, const uint32_t *face_verts, const int64_t *face_start,
+                       const int32_t *face_group, int64_t n_faces, wh_mesh_room **out);
+void wh_mesh_room_free(wh_mesh_room *room);
+int32_t wh_mesh_room_surface_count(const wh_mesh_room *room);
+int64_t wh_mesh_room_triangle_count(const wh_mesh_room *room);
+/* Surface s: its material group, kind (0 wall, 1 floor, 2 ceiling), unit
+ * normal into the room, plane offset d = n.p and area.  Any output may be
+ * NULL. */
+void wh_mesh_room_surface(const wh_mesh_room *room, int32_t s, int32_t *group, int32_t *kind, double normal[3],
+                          double *d, double *area);
+/* positions [triangles][3][3] (wound to their surface's normal) and the
+ * surface of each triangle (Room::tri_surface). */
+void wh_mesh_room_triangles(const wh_mesh_room *room, double *positions, uint32_t *tri_surface);
+void wh_mesh_room_bounds(const wh_mesh_room *room, double lo[3], double hi[3]);
+/* Room::contains for mesh rooms (room.rs:151-157, parity_inside). */
+int wh_mesh_room_contains(const wh_mesh_room *room, const double p[3]);
+/* Room::volume (room.rs:165-178). */
+double wh_mesh_room_volume(const wh_mesh_room *room);
+
 /* ------------------------------------------------------------------- grids
  * FdtdGrid (fdtd.rs:196-209) with the boundary nodes in CSR form.
  */
@@ -108,6 +138,14 @@ typedef struct {
 /* FdtdGrid::build_dx (fdtd.rs:289-378) with `fits` holding one fit per
  * surface.  Fails with WAVEY_E_LIMIT above MAX_CELLS. */
 int wh_grid_build(const wh_room *room, const wh_fit *fits, int32_t n_fits, double c, double dx, wh_grid **out);
+/* FdtdGrid::build_dx (fdtd.rs:289-378) for a mesh room: air by column_fill
+ * (fdtd.rs:385-422, one upward ray per grid column), the surface behind
+ * each missing face by the closest triangle along the face direction within
+ * 1.5 dx (fdtd.rs:357-362).  solids: optional rigid boxes [n_solids][6]
+ * (x0, y0, z0, x1, y1, z1) whose faces carry no admittance.  fits: one per
+ * surface (wh_mesh_room_surface_count). */
+int wh_grid_build_mesh(const wh_mesh_room *room, const double *solids, int32_t n_solids, const wh_fit *fits,
+                       int32_t n_fits, double c, double dx, wh_grid **out);
 /* FdtdGrid::build_with spacing rule (fdtd.rs:282-286): c / (f_max * ppw),
  * at most the smallest solid side / 8. */
 double wh_grid_spacing(const wh_room *room, double c, double f_max, double ppw);

@@ -116,13 +116,20 @@ class FdtdGrid:
 
     # -------------------------------------------------------------- build
     @staticmethod
-    def build_dx(room: BoxRoom, fits: list, c: float, dx: float) -> "FdtdGrid":
+    def build_dx(room, fits: list, c: float, dx: float, solids=()) -> "FdtdGrid":
+        """room: a BoxRoom, or a MeshRoom (with optional rigid boxes
+        `solids`, (x0, y0, z0, x1, y1, z1) each)."""
         if len(fits) != room.n_surfaces:
             raise ValueError(f"{len(fits)} fits for {room.n_surfaces} surfaces")
-        r, keep = room._c()
         arr = (N.WhFit * len(fits))(*[f._c() for f in fits])
         out = C.c_void_p()
-        st = N.host().wh_grid_build(C.byref(r), arr, len(fits), float(c), float(dx), C.byref(out))
+        if hasattr(room, "_h"):  # MeshRoom
+            sol = np.ascontiguousarray(np.asarray(solids, dtype=np.float64).reshape(-1, 6))
+            st = N.host().wh_grid_build_mesh(room._h, N.ptr(sol, C.c_double) if len(sol) else None, len(sol), arr,
+                                             len(fits), float(c), float(dx), C.byref(out))
+        else:
+            r, keep = room._c()
+            st = N.host().wh_grid_build(C.byref(r), arr, len(fits), float(c), float(dx), C.byref(out))
         if st == N.WAVEY_E_LIMIT:
             raise ValueError("the wave solver grid would exceed MAX_CELLS; lower the crossover frequency")
         if st != 0:
@@ -130,7 +137,14 @@ class FdtdGrid:
         return FdtdGrid(out.value)
 
     @staticmethod
-    def build(room: BoxRoom, fits: list, c: float, f_max: float, ppw: float) -> "FdtdGrid":
+    def build(room, fits: list, c: float, f_max: float, ppw: float, solids=()) -> "FdtdGrid":
+        """FdtdGrid::build / build_with (fdtd.rs:276-286): dx = c / (f_max
+        ppw), at most the smallest solid side / 8."""
+        if hasattr(room, "_h"):  # MeshRoom
+            dx = float(c) / (float(f_max) * float(ppw))
+            for s in solids:
+                dx = min(dx, min(s[3] - s[0], s[4] - s[1], s[5] - s[2]) / 8.0)
+            return FdtdGrid.build_dx(room, fits, c, dx, solids)
         r, keep = room._c()
         dx = N.host().wh_grid_spacing(C.byref(r), float(c), float(f_max), float(ppw))
         return FdtdGrid.build_dx(room, fits, c, dx)
