@@ -76,3 +76,51 @@ def test_every_tma_shape_agrees(backend, library, precision, cfg):
             del os.environ["WAVEY_TMA_CFG"], os.environ["WAVEY_TMA_ZT"]
         assert np.array_equal(ir, ref[1]), (cfg, zt)
         assert np.array_equal(spec, ref[0]), (cfg, zt)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+@pytest.mark.parametrize("cfg", range(7))
+def test_special_cells_inside_the_march_agree(backend, library, lanes, cfg):
+    """The fused form (WAVEY_BRANCH=9: every interior CTA also updates the
+    special cells of its tile from the staged planes) gives the register-
+    queue kernel's results bit for bit, for every tile shape, z-runs of 1, 3
+    and 64 planes, and 1, 2 or 4 lanes per cell: rigid faces, boundary nodes
+    with branch states, and merged source taps."""
+    g, taps, sig, rcv, freqs = branch_room(library, 0.1)
+    comps = directional_components(g, (1.6, 1.3, 1.1))
+    sources = (comps + [taps])[:lanes] if lanes < 4 else comps + [taps]
+    os.environ["WAVEY_INTERIOR"] = "regq"
+    try:
+        ref = backend.run_batch(g, sources, sig, rcv, freqs, precision=FP32, ir=True)
+    finally:
+        del os.environ["WAVEY_INTERIOR"]
+    for zt in (1, 3, 64):
+        os.environ.update(WAVEY_TMA_CFG=str(cfg), WAVEY_TMA_ZT=str(zt), WAVEY_BRANCH="9")
+        try:
+            plan = backend.plan(g, sources, sig, rcv, freqs, precision=FP32, ir=True)
+            info = plan.info()
+            assert (info["tma_depth"], info["tma_zt"], info["branch"]) == (cfg, zt, 9)
+            plan.run()
+            spec, ir = plan.read()
+            plan.close()
+        finally:
+            for k in ("WAVEY_TMA_CFG", "WAVEY_TMA_ZT", "WAVEY_BRANCH"):
+                del os.environ[k]
+        assert np.array_equal(ir, ref[1]), (cfg, zt)
+        assert np.array_equal(spec, ref[0]), (cfg, zt)
+
+
+def test_fused_form_on_the_pillar_room(backend):
+    """The fused form on a room with pillars and a spread source (taps on
+    several cells of one tile), against the concurrent-branch form."""
+    from scenes import pillar_room
+
+    g, taps, sig, rcv, freqs = pillar_room(0.2)
+    ref = backend.run_batch(g, [taps, taps], sig, rcv, freqs, precision=FP32, ir=True)
+    os.environ["WAVEY_BRANCH"] = "9"
+    try:
+        got = backend.run_batch(g, [taps, taps], sig, rcv, freqs, precision=FP32, ir=True)
+    finally:
+        del os.environ["WAVEY_BRANCH"]
+    assert np.array_equal(got[1], ref[1])
+    assert np.array_equal(got[0], ref[0])

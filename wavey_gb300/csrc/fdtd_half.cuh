@@ -179,6 +179,7 @@ __device__ __forceinline__ float warp_max(float m) {
 // inverse of level n+1's on store, which also raises the slab maximum.
 template <int V>
 struct HalfField {
+    static constexpr bool STREAM = false;
     const __half *P;
     __half *Q;
     float sm, sc, sp, so, inv;
@@ -186,6 +187,9 @@ struct HalfField {
     mutable float mx;  // max |p^(n+1)| stored, for the slab maximum
     __device__ __forceinline__ Lanes<float, V> p(long long cell, int dz) const {
         return load_h<V>(P + cell * V, dz < 0 ? sm : (dz > 0 ? sp : sc));
+    }
+    __device__ __forceinline__ Lanes<float, V> nb(long long cell, int d, long long off) const {
+        return p(cell + off, d == 4 ? -1 : (d == 5 ? 1 : 0));
     }
     __device__ __forceinline__ Lanes<float, V> old(long long cell) const { return load_h<V>(Q + cell * V, so); }
     __device__ __forceinline__ void put(long long cell, const Lanes<float, V> &v) const {

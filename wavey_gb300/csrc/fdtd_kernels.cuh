@@ -181,12 +181,18 @@ __device__ __forceinline__ void load_slot(const A &a, const T *SU, const T *SG, 
 
 // Field access of the special-cell update for values stored as computed
 // (FP32, FP64): p^n at a cell (dz: its plane relative to the cell's, which
-// FP16 storage needs for the slab scale), p^(n-1), and the store of p^(n+1).
+// FP16 storage needs for the slab scale), p^n at its neighbour d (-x, +x,
+// -y, +y, -z, +z; off: the neighbour's cell offset), p^(n-1), and the store
+// of p^(n+1).
 template <class T, int V>
 struct PlainField {
+    static constexpr bool STREAM = false;
     const T *P;
     T *Q;
     __device__ __forceinline__ Lanes<T, V> p(long long cell, int) const { return load<T, V, true>(P + cell * V); }
+    __device__ __forceinline__ Lanes<T, V> nb(long long cell, int, long long off) const {
+        return load<T, V, true>(P + (cell + off) * V);
+    }
     __device__ __forceinline__ Lanes<T, V> old(long long cell) const { return load<T, V, false>(Q + cell * V); }
     __device__ __forceinline__ void put(long long cell, const Lanes<T, V> &v) const { store<T, V>(Q + cell * V, v); }
 };
@@ -208,25 +214,44 @@ __device__ __forceinline__ void special_core(const A &a, const F &f, const uint4
     const Lanes<T, V> pc = f.p(cell, 0);
     const Lanes<T, V> pp = f.old(cell);
     const long long offs[6] = {-1, 1, -(long long)a.nxp, (long long)a.nxp, -nxy, nxy};
-    Lanes<T, V> nb[6];
-#pragma unroll
-    for (int d = 0; d < 6; d++)
-        if ((m >> d) & 1u) nb[d] = f.p(cell + offs[d], d == 4 ? -1 : (d == 5 ? 1 : 0));
-    SlotRegs<T, V> sr[SR > 0 ? SR : 1];
-#pragma unroll
-    for (int q = 0; q < SR; q++)
-        if (q < ns) load_slot<T, V, A>(a, SU, SG, j0 + q, sr[q]);
     // The laplacian over air neighbours in the -x,+x,-y,+y,-z,+z order.
+    // Fields in global memory load every neighbour before summing (one
+    // round of memory latency); fields staged in shared memory (F::STREAM)
+    // sum each neighbour as it is read, which holds fewer registers.  The
+    // sums and their order are the same.
     Lanes<T, V> sum;
 #pragma unroll
     for (int l = 0; l < V; l++) sum.v[l] = T(0);
     T kk = T(0);
+    SlotRegs<T, V> sr[SR > 0 ? SR : 1];
+    if constexpr (F::STREAM) {
 #pragma unroll
-    for (int d = 0; d < 6; d++) {
-        if ((m >> d) & 1u) {
+        for (int d = 0; d < 6; d++) {
+            if ((m >> d) & 1u) {
+                const Lanes<T, V> v = f.nb(cell, d, offs[d]);
 #pragma unroll
-            for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb[d].v[l]);
-            kk = radd(kk, T(1));
+                for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], v.v[l]);
+                kk = radd(kk, T(1));
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < SR; q++)
+            if (q < ns) load_slot<T, V, A>(a, SU, SG, j0 + q, sr[q]);
+    } else {
+        Lanes<T, V> nb[6];
+#pragma unroll
+        for (int d = 0; d < 6; d++)
+            if ((m >> d) & 1u) nb[d] = f.nb(cell, d, offs[d]);
+#pragma unroll
+        for (int q = 0; q < SR; q++)
+            if (q < ns) load_slot<T, V, A>(a, SU, SG, j0 + q, sr[q]);
+#pragma unroll
+        for (int d = 0; d < 6; d++) {
+            if ((m >> d) & 1u) {
+#pragma unroll
+                for (int l = 0; l < V; l++) sum.v[l] = radd(sum.v[l], nb[d].v[l]);
+                kk = radd(kk, T(1));
+            }
         }
     }
     Lanes<T, V> lap, next;

@@ -29,6 +29,17 @@
 // fdtd_step_half's interior role in the same order, so the two give identical
 // results.
 //
+// With SPEC (FP32 only) the CTA also updates the special cells of its tile:
+// after the interior cells of plane z it takes the tile's special cells of
+// that plane from a list ordered by (tile, plane) and runs the special-cell
+// update on them -- rigid faces, boundary nodes with their branch states,
+// source taps -- reading p^n and p^(n-1) from the rings it already holds
+// (every neighbour of a tile cell lies in the staged planes and halos) and
+// the slot constants and branch states from global memory.  The special work
+// then rides on the interior's bytes in flight instead of a separate kernel
+// whose dependent load chains run after the interior's.  The update is
+// special_core's, so results do not change by a bit.
+//
 // Every wait on an mbarrier is bounded.  If one runs out, the kernel records
 // the failure in the error word, waits (again bounded) for the copies it has
 // issued, and returns; the host reports WAVEY_E_DEVICE.
@@ -127,6 +138,135 @@ __device__ __forceinline__ void ld4u(const __half *p, float o[4]) {
     o[3] = __high2float(b);
 }
 
+// Field access of the special-cell update from the staged planes (FP32): the
+// cell's element in the p^n planes z, z - 1 and z + 1 and in the p^(n-1)
+// plane, all in shared memory, and the global store of p^(n+1).
+template <int V>
+__device__ __forceinline__ Lanes<float, V> lds(const float *p) {
+    Lanes<float, V> o;
+    if constexpr (V == 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(p);
+        o.v[0] = v.x, o.v[1] = v.y, o.v[2] = v.z, o.v[3] = v.w;
+    } else if constexpr (V == 2) {
+        const float2 v = *reinterpret_cast<const float2 *>(p);
+        o.v[0] = v.x, o.v[1] = v.y;
+    } else {
+        o.v[0] = *p;
+    }
+    return o;
+}
+
+template <int V>
+struct SmemField {
+    static constexpr bool STREAM = true;
+    const float *c, *zm, *zp, *q;  // the cell in p^n planes z, z-1, z+1 and in the p^(n-1) plane
+    int prow;                      // elements per staged p row
+    float *Q;                      // the chunk's p^(n-1) / p^(n+1) field in global memory
+    __device__ __forceinline__ Lanes<float, V> p(long long, int) const { return lds<V>(c); }
+    __device__ __forceinline__ Lanes<float, V> nb(long long, int d, long long) const {
+        return lds<V>(d == 0 ? c - V : d == 1 ? c + V : d == 2 ? c - prow : d == 3 ? c + prow : d == 4 ? zm : zp);
+    }
+    __device__ __forceinline__ Lanes<float, V> old(long long) const { return lds<V>(q); }
+    __device__ __forceinline__ void put(long long cell, const Lanes<float, V> &v) const { store<float, V>(Q + cell * V, v); }
+};
+
+// One right-hand side (lane l) of a special cell, from the staged planes:
+// special_core's FP32 arithmetic (shader order) for a single lane.  A
+// cell's V lanes run on V neighbouring threads, so each thread holds one
+// lane's values: the constants and branch states of up to SLOT_REGS slots
+// are loaded together, before the neighbour sums, in one round of memory
+// latency.  Every lane computes the cell's s1 and denominator itself, with
+// the same operations, so the lanes agree with the V-wide update bit for bit.
+template <int V>
+__device__ __forceinline__ void special_lane(const StepArgs<float> &a, const SmemField<V> &f, const uint4 rec, int c,
+                                             int l, long long n) {
+    const uint32_t m = rec.y;
+    const long long j0 = rec.z;
+    const uint32_t tap = rec.w;
+    const int ns = (int)((m >> META_SLOT_SHIFT) & META_SLOT_MASK);
+    float *SU = a.su + (long long)c * a.n_slots * V + l;
+    float *SG = a.sg + (long long)c * a.n_slots * V + l;
+    const float4 *K = reinterpret_cast<const float4 *>(a.slots);
+    float4 k[SLOT_REGS];
+    float u[SLOT_REGS], g[SLOT_REGS];
+#pragma unroll
+    for (int q = 0; q < SLOT_REGS; q++)
+        if (q < ns) {
+            k[q] = __ldg(K + j0 + q);
+            u[q] = SU[(j0 + q) * V];
+            g[q] = SG[(j0 + q) * V];
+        }
+    const float pc = f.c[l], pp = f.q[l];
+    float sum = 0.0f, kk = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 6; d++)
+        if ((m >> d) & 1u) {
+            const float *nb = d == 0 ? f.c - V : d == 1 ? f.c + V : d == 2 ? f.c - f.prow : d == 3 ? f.c + f.prow
+                            : d == 4 ? f.zm : f.zp;
+            sum = radd(sum, nb[l]);
+            kk = radd(kk, 1.0f);
+        }
+    const float lap = rmul(a.l2, rsub(sum, rmul(kk, pc)));
+    float next;
+    if (ns == 0) {
+        next = radd(rsub(rmul(2.0f, pc), pp), lap);
+    } else {
+        float s1 = 0.0f, s2 = 0.0f;
+        for (int q = 0; q < ns; q++) {
+            float4 kq;
+            float uq, gq;
+            if (q < SLOT_REGS) {
+#pragma unroll
+                for (int i = 0; i < SLOT_REGS; i++)
+                    if (i == q) kq = k[i], uq = u[i], gq = g[i];
+            } else {
+                kq = __ldg(K + j0 + q);
+                uq = SU[(j0 + q) * V];
+                gq = SG[(j0 + q) * V];
+            }
+            // kq = (inv_d, cv, k, w)
+            const float e = rmul(radd(radd(rsub(rmul(kq.y, uq), rmul(kq.z, gq)), rmul(0.5f, pc)), rmul(kq.w, pp)), kq.x);
+            s2 = rsub(radd(s2, e), uq);
+            s1 = radd(s1, rmul(rsub(0.5f, kq.w), kq.x));
+        }
+        const float den = radd(1.0f, rmul(a.lam, s1));
+        next = rdiv(rsub(radd(rsub(rmul(2.0f, pc), pp), lap), rmul(a.lam, s2)), den);
+        for (int q = 0; q < ns; q++) {
+            float4 kq;
+            float uq, gq;
+            if (q < SLOT_REGS) {
+#pragma unroll
+                for (int i = 0; i < SLOT_REGS; i++)
+                    if (i == q) kq = k[i], uq = u[i], gq = g[i];
+            } else {
+                kq = __ldg(K + j0 + q);
+                uq = SU[(j0 + q) * V];
+                gq = SG[(j0 + q) * V];
+            }
+            const float e = rmul(radd(radd(rsub(rmul(kq.y, uq), rmul(kq.z, gq)), rmul(0.5f, pc)), rmul(kq.w, pp)), kq.x);
+            const float un = radd(rmul(rmul(rsub(0.5f, kq.w), kq.x), next), e);
+            SG[(j0 + q) * V] = radd(gq, rmul(a.half_dt, radd(un, uq)));
+            SU[(j0 + q) * V] = un;
+        }
+    }
+    if (tap != NO_TAP) {
+        const int s = c * V + l;
+        next = radd(next, rmul(a.sig[(long long)s * a.sig_stride + n], a.tapw[(long long)tap * a.lanes_total + s]));
+    }
+    f.Q[(long long)rec.x * V + l] = next;
+}
+
+// The special cells of every tile, for the SPEC form: records (as in
+// StepArgs::sp) ordered by (tile row ty, tile column tx, z, y, x); off[(ty *
+// tiles_x + tx) * nz + z] is the first record of that tile and plane, and the
+// next entry ends it.  a carries the update's slots, branch states, taps and
+// signals.
+struct SpecTile {
+    const uint4 *rec;
+    const uint32_t *off;
+    StepArgs<float> a;
+};
+
 // V: sources per cell in a chunk (1, 2 or 4); a tile row holds 128 / V cells.
 // R: rows per tile (8 or 16; 256 threads, R / 8 rows per thread).
 // NP / NQ: planes in the two rings; NP - 3 p planes and NQ - 1 old planes are
@@ -141,16 +281,22 @@ __host__ __device__ constexpr uint32_t tma_q_bytes() { return TMA_ROW_FLOATS * R
 // FP16 plans are at most TMA_MAX_ZT planes).
 constexpr int TMA_MAX_ZT = 64;
 constexpr int TMA_SCALE_STRIDE = TMA_MAX_ZT + 2;
-template <class E>
-__host__ __device__ constexpr uint32_t tma_scale_bytes() { return sizeof(E) == 2 ? 4 * TMA_SCALE_STRIDE * 4 : 0; }
-template <class E, int R, int NP, int NQ>
+// SPEC: the first special record of each plane of the z-run (z-runs of
+// SPEC plans are at most TMA_MAX_ZT planes too).
+template <class E, bool SPEC>
+__host__ __device__ constexpr uint32_t tma_scale_bytes() {
+    return sizeof(E) == 2 ? 4 * TMA_SCALE_STRIDE * 4 : SPEC ? TMA_SCALE_STRIDE * 4 : 0;
+}
+template <class E, int R, int NP, int NQ, bool SPEC = false>
 __host__ __device__ constexpr uint32_t tma_smem_of() {
-    return NP * tma_p_stride<E, R>() + NQ * tma_q_bytes<E, R>() + 256 + tma_scale_bytes<E>() + 128;
+    return NP * tma_p_stride<E, R>() + NQ * tma_q_bytes<E, R>() + 256 + tma_scale_bytes<E, SPEC>() + 128;
 }
 
-template <class E, int V, int R, int NP, int NQ>
-__global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUtensorMap tm_p,
-                                                    const __grid_constant__ CUtensorMap tm_q, TmaArgs<E> a) {
+template <class E, int V, int R, int NP, int NQ, bool SPEC = false>
+__global__ void __launch_bounds__(256, SPEC ? 3 : 1) interior_tma(const __grid_constant__ CUtensorMap tm_p,
+                                                    const __grid_constant__ CUtensorMap tm_q, TmaArgs<E> a,
+                                                    const __grid_constant__ SpecTile sp) {
+    static_assert(!SPEC || sizeof(E) == 4, "special cells inside the march: FP32 fields only");
     constexpr bool HALF = sizeof(E) == 2;
     constexpr int RT = R / 8;                    // rows per thread
     constexpr int HALO = tma_halo<E>(), PROW = tma_p_row<E>();
@@ -201,6 +347,13 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
                 __uint_as_float(min(__float_as_uint(65504.0f * s_new[zs + i].x), 0x7f7fffffu));
         }
     }
+    // SPEC: the first special record of planes zs..ze of this tile (the last
+    // one ends plane ze - 1), staged once.
+    uint32_t *soff = reinterpret_cast<uint32_t *>(base + NP * PS + NQ * QB + 256);
+    if constexpr (SPEC) {
+        const uint32_t *src = sp.off + ((long long)ty * a.tiles_x + tx) * a.nz + zs;
+        for (int i = threadIdx.x; i <= Kq; i += 256) soff[i] = __ldg(src + i);
+    }
     if (threadIdx.x == 0) {
         for (int i = 0; i < NP + NQ; i++) mbar_init(smem_addr(bars + i), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -228,6 +381,7 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
 
     const int x0 = tx * CELLS + lane * (4 / V);
     E *Q = a.nxt + (long long)c * a.cells_p * V;
+    const long long nstep = SPEC ? *a.base + a.t : 0;  // SPEC: the step (signals are indexed by it)
     const long long mstep = (long long)a.ny * a.nxw;
     // FP16: the maxima slot of level n+1, and the scales of planes j and j+1.
     unsigned int *amax_new = nullptr;
@@ -345,6 +499,26 @@ __global__ void __launch_bounds__(256) interior_tma(const __grid_constant__ CUte
                         if ((bits >> q) & 1u)
 #pragma unroll
                             for (int l = 0; l < V; l++) dst[q * V + l] = nx4[q * V + l];
+                }
+            }
+            if constexpr (SPEC) {
+                // The tile's special cells of plane z, from the same staged
+                // planes: one thread per (cell, lane), a cell's lanes on
+                // neighbouring threads.
+                const uint32_t k0 = soff[j], tasks = (soff[j + 1] - k0) * V;
+                for (uint32_t t = threadIdx.x; t < tasks; t += 256) {
+                    const uint4 rec = __ldg(sp.rec + k0 + t / V);
+                    const int l = (int)(t % V);
+                    const uint32_t xg = rec.x % (uint32_t)a.nxp;
+                    const int row = (int)((rec.x / (uint32_t)a.nxp) % (uint32_t)a.ny) - y0;
+                    const int e0 = ((int)xg - tx * CELLS) * V;
+                    const int at = (row + 1) * PROW + HALO + e0;
+                    const SmemField<V> f{reinterpret_cast<const float *>(pc) + at,
+                                         reinterpret_cast<const float *>(pm) + at,
+                                         reinterpret_cast<const float *>(pn) + at,
+                                         reinterpret_cast<const float *>(qo) + row * TMA_ROW_FLOATS + e0, PROW,
+                                         reinterpret_cast<float *>(Q)};
+                    special_lane<V>(sp.a, f, rec, c, l, nstep);
                 }
             }
         }

@@ -81,6 +81,9 @@ int env_int(const char *name, int dflt, int lo, int hi) {
 struct wavey_cuda_ctx {
     int device = 0;
     int sm_count = 0;
+    int max_persist_l2 = 0;     // bytes of L2 that may be set aside for persisting accesses
+    int max_window = 0;         // largest access-policy window
+    size_t persist_set = 0;     // persisting set-aside requested so far by this context's plans
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;  // the special-cell branch of a TMA step
     std::mutex mu;
@@ -146,7 +149,18 @@ struct wavey_cuda_plan {
     CUtensorMap tm_p[2], tm_q[2];  // per parity: p^n of field[parity], old of field[parity^1]
     int tma_tiles_x = 0, tma_tiles_y = 0, tma_tiles_z = 0, tma_zt = 32, tma_blocks = 0;
     int tma_cfg = 0;      // shape of the TMA kernel, an index into TMA_CFGS
-    int branch = 0;             // special-cell branch form: register cap (branch / 3) and priority (branch % 3)
+    int branch = 0;             // special-cell form: branch < 9: a concurrent kernel with register cap
+                                // (branch / 3) and priority (branch % 3); BRANCH_FUSED: inside the interior CTAs
+    std::vector<uint4> sp_host;   // special records in cell order (host copy, for the tile orders)
+    // The special cells' records, slot constants and branch states in one
+    // block, kept resident in L2 across steps by a persisting access-policy
+    // window on the special-cell kernel (the field streams would otherwise
+    // evict them every step).
+    void *l2_block = nullptr;
+    size_t l2_block_bytes = 0;
+    cudaAccessPolicyWindow l2_window = {};
+    uint4 *sp_tile[3] = {nullptr, nullptr, nullptr};     // per tile height 8, 16, 32: records by (tile, plane)
+    uint32_t *sp_off[3] = {nullptr, nullptr, nullptr};   // and the first record of each (tile, plane)
     int prio_lo = 0, prio_hi = 0;
     int *err = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
@@ -158,6 +172,8 @@ struct wavey_cuda_plan {
 
     ~wavey_cuda_plan() {
         if (graph) cudaGraphExecDestroy(graph);
+        // Lines of the freed special block would keep their persisting state.
+        if (l2_window.num_bytes) cudaCtxResetPersistingL2Cache();
         for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1, inflight[0], inflight[1], inflight[2], inflight[3], ev_fork, ev_join})
             if (e) cudaEventDestroy(e);
         for (DevBuf &b : bufs)
@@ -302,51 +318,65 @@ struct TmaCfg {
 };
 constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4}, {8, 8, 4}, {16, 6, 4}, {16, 8, 4}, {16, 5, 3}, {32, 5, 3}, {32, 4, 2}};
 constexpr int TMA_NCFG = 7;
+// Special-cell form in which the interior CTAs update the special cells of
+// their tiles (FP32 plans); forms 0-8 run them in a concurrent kernel.
+constexpr int BRANCH_FUSED = 9;
 
-template <class E, int V, int R, int NP, int NQ>
+// Index of a tile height (8, 16 or 32 rows) in the plan's tile-ordered special lists.
+inline int tile_slot(int rows) { return rows == 8 ? 0 : rows == 16 ? 1 : 2; }
+
+template <class E, int V, int R, int NP, int NQ, bool SPEC>
 void launch_tma(int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
-                const wk::TmaArgs<E> &ta) {
+                const wk::TmaArgs<E> &ta, const wk::SpecTile &sp) {
     cudaLaunchConfig_t lc = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributePriority;
     attr[0].val.priority = prio;
     lc.gridDim = dim3(blocks);
     lc.blockDim = dim3(256);
-    lc.dynamicSmemBytes = wk::tma_smem_of<E, R, NP, NQ>();
+    lc.dynamicSmemBytes = wk::tma_smem_of<E, R, NP, NQ, SPEC>();
     lc.stream = s;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    cudaLaunchKernelEx(&lc, wk::interior_tma<E, V, R, NP, NQ>, p, q, ta);
+    cudaLaunchKernelEx(&lc, wk::interior_tma<E, V, R, NP, NQ, SPEC>, p, q, ta, sp);
 }
 
-template <class E, int V>
+template <class E, int V, bool SPEC>
 void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
-                    const wk::TmaArgs<E> &ta) {
+                    const wk::TmaArgs<E> &ta, const wk::SpecTile &sp) {
     switch (cfg) {
-        case 1: launch_tma<E, V, 8, 8, 4>(blocks, s, prio, p, q, ta); break;
-        case 2: launch_tma<E, V, 16, 6, 4>(blocks, s, prio, p, q, ta); break;
-        case 3: launch_tma<E, V, 16, 8, 4>(blocks, s, prio, p, q, ta); break;
-        case 4: launch_tma<E, V, 16, 5, 3>(blocks, s, prio, p, q, ta); break;
-        case 5: launch_tma<E, V, 32, 5, 3>(blocks, s, prio, p, q, ta); break;
-        case 6: launch_tma<E, V, 32, 4, 2>(blocks, s, prio, p, q, ta); break;
-        default: launch_tma<E, V, 8, 6, 4>(blocks, s, prio, p, q, ta); break;
+        case 1: launch_tma<E, V, 8, 8, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
+        case 2: launch_tma<E, V, 16, 6, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
+        case 3: launch_tma<E, V, 16, 8, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
+        case 4: launch_tma<E, V, 16, 5, 3, SPEC>(blocks, s, prio, p, q, ta, sp); break;
+        case 5: launch_tma<E, V, 32, 5, 3, SPEC>(blocks, s, prio, p, q, ta, sp); break;
+        case 6: launch_tma<E, V, 32, 4, 2, SPEC>(blocks, s, prio, p, q, ta, sp); break;
+        default: launch_tma<E, V, 8, 6, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
     }
 }
 
-template <class E, int V, int R, int NP, int NQ>
+template <class E, int V, int R, int NP, int NQ, bool SPEC>
 cudaError_t tma_attr() {
-    return cudaFuncSetAttribute((const void *)wk::interior_tma<E, V, R, NP, NQ>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wk::tma_smem_of<E, R, NP, NQ>());
+    return cudaFuncSetAttribute((const void *)wk::interior_tma<E, V, R, NP, NQ, SPEC>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wk::tma_smem_of<E, R, NP, NQ, SPEC>());
+}
+
+template <class E, int V, bool SPEC>
+cudaError_t tma_attrs_spec() {
+    cudaError_t e[] = {tma_attr<E, V, 8, 6, 4, SPEC>(),  tma_attr<E, V, 8, 8, 4, SPEC>(),  tma_attr<E, V, 16, 6, 4, SPEC>(),
+                       tma_attr<E, V, 16, 8, 4, SPEC>(), tma_attr<E, V, 16, 5, 3, SPEC>(), tma_attr<E, V, 32, 5, 3, SPEC>(),
+                       tma_attr<E, V, 32, 4, 2, SPEC>()};
+    for (cudaError_t x : e)
+        if (x != cudaSuccess) return x;
+    return cudaSuccess;
 }
 
 template <class E, int V>
 cudaError_t tma_attrs() {
-    cudaError_t e[] = {tma_attr<E, V, 8, 6, 4>(), tma_attr<E, V, 8, 8, 4>(), tma_attr<E, V, 16, 6, 4>(),
-                       tma_attr<E, V, 16, 8, 4>(), tma_attr<E, V, 16, 5, 3>(), tma_attr<E, V, 32, 5, 3>(),
-                       tma_attr<E, V, 32, 4, 2>()};
-    for (cudaError_t x : e)
-        if (x != cudaSuccess) return x;
-    return cudaSuccess;
+    cudaError_t e = tma_attrs_spec<E, V, false>();
+    if constexpr (sizeof(E) == 4)
+        if (e == cudaSuccess) e = tma_attrs_spec<E, V, true>();
+    return e;
 }
 
 // The TMA kernel's arguments for one step (FP16 fields are unused in FP32).
@@ -377,7 +407,15 @@ wk::TmaArgs<E> tma_args(const wavey_cuda_plan *pl, int t, int parity) {
 template <int V>
 void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
     cudaStream_t s = pl->ctx->stream, side = pl->ctx->side;
-    const bool branch = pl->special_blocks + pl->record_blocks > 0;
+    const bool fused = pl->branch == BRANCH_FUSED;
+    const bool branch = (fused ? 0 : pl->special_blocks) + pl->record_blocks > 0;
+    wk::SpecTile sp = {};
+    if (fused) {
+        const int slot = tile_slot(TMA_CFGS[pl->tma_cfg].rows);
+        sp.rec = pl->sp_tile[slot];
+        sp.off = pl->sp_off[slot];
+        fill_args<float>(pl, sp.a, parity);
+    }
     if (branch) {
         // Special cells and receiver samples on a concurrent branch (the fused
         // kernel's special and record roles): they read only p^n and write
@@ -388,23 +426,29 @@ void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
         fill_args<float>(pl, a, parity);
         a.interior_blocks = 0;
         cudaLaunchConfig_t lc = {};
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributePriority;
         attr[0].val.priority = pl->branch % 3 == 1 ? pl->prio_hi : pl->prio_lo;
+        attr[1].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[1].val.accessPolicyWindow = pl->l2_window;
         lc.blockDim = dim3(wk::BLOCK);
         lc.stream = side;
         lc.attrs = attr;
-        lc.numAttrs = 1;
-        lc.gridDim = dim3(pl->special_blocks + pl->record_blocks);
-        switch (pl->branch / 3) {
+        lc.numAttrs = pl->l2_window.num_bytes ? 2 : 1;
+        if (fused) a.special_blocks = 0;  // receivers only: the special cells run inside the interior CTAs
+        lc.gridDim = dim3(a.special_blocks + pl->record_blocks);
+        switch (fused ? 0 : pl->branch / 3) {
             case 1: cudaLaunchKernelEx(&lc, wk::special_branch<V, 3>, a, t); break;
             case 2: cudaLaunchKernelEx(&lc, wk::special_branch<V, 4>, a, t); break;
             default: cudaLaunchKernelEx(&lc, wk::special_branch<V, 1>, a, t); break;
         }
     }
-    if (pl->tma_blocks > 0)
-        launch_tma_cfg<float, V>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
-                                 pl->tm_p[parity], pl->tm_q[parity], tma_args<float>(pl, t, parity));
+    if (pl->tma_blocks > 0 && fused)
+        launch_tma_cfg<float, V, true>(pl->tma_cfg, pl->tma_blocks, s, pl->prio_lo, pl->tm_p[parity], pl->tm_q[parity],
+                                       tma_args<float>(pl, t, parity), sp);
+    else if (pl->tma_blocks > 0)
+        launch_tma_cfg<float, V, false>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
+                                        pl->tm_p[parity], pl->tm_q[parity], tma_args<float>(pl, t, parity), sp);
     if (branch) {
         cudaEventRecord(pl->ev_join, side);
         cudaStreamWaitEvent(s, pl->ev_join, 0);
@@ -478,14 +522,16 @@ void launch_step_half_tma(wavey_cuda_plan *pl, int t, int parity) {
         cudaEventRecord(pl->ev_fork, s);
         cudaStreamWaitEvent(side, pl->ev_fork, 0);
         cudaLaunchConfig_t lc = {};
-        cudaLaunchAttribute attr[1];
+        cudaLaunchAttribute attr[2];
         attr[0].id = cudaLaunchAttributePriority;
         attr[0].val.priority = pl->branch % 3 == 1 ? pl->prio_hi : pl->prio_lo;
+        attr[1].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[1].val.accessPolicyWindow = pl->l2_window;
         lc.blockDim = dim3(wk::BLOCK);
         lc.gridDim = dim3(blocks);
         lc.stream = side;
         lc.attrs = attr;
-        lc.numAttrs = 1;
+        lc.numAttrs = pl->l2_window.num_bytes ? 2 : 1;
         switch (pl->branch / 3) {
             case 1: cudaLaunchKernelEx(&lc, wk::special_branch_half<V, 3>, a, t); break;
             case 2: cudaLaunchKernelEx(&lc, wk::special_branch_half<V, 4>, a, t); break;
@@ -493,8 +539,9 @@ void launch_step_half_tma(wavey_cuda_plan *pl, int t, int parity) {
         }
     }
     if (pl->tma_blocks > 0)
-        launch_tma_cfg<__half, V>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
-                                  pl->tm_p[parity], pl->tm_q[parity], tma_args<__half>(pl, t, parity));
+        launch_tma_cfg<__half, V, false>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
+                                         pl->tm_p[parity], pl->tm_q[parity], tma_args<__half>(pl, t, parity),
+                                         wk::SpecTile{});
     if (blocks > 0) {
         cudaEventRecord(pl->ev_join, side);
         cudaStreamWaitEvent(s, pl->ev_join, 0);
@@ -626,6 +673,74 @@ int upload_typed(wavey_cuda_plan *pl, void **out, const std::vector<double> &src
     return pl->ctx->cuda(cudaStreamSynchronize(pl->ctx->stream), "upload sync");
 }
 
+// Converts src to T into an existing device buffer and waits for the copy.
+template <class T>
+int upload_into(wavey_cuda_plan *pl, void *dst, const std::vector<double> &src) {
+    std::vector<T> v = convert<T>(src.data(), src.size());
+    pl->h2d_bytes += (int64_t)(v.size() * sizeof(T));
+    if (v.empty()) return WAVEY_OK;
+    int st = pl->ctx->cuda(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, pl->ctx->stream),
+                           "upload");
+    if (st) return st;
+    return pl->ctx->cuda(cudaStreamSynchronize(pl->ctx->stream), "upload sync");
+}
+
+// The persisting L2 window over the plan's special block (records, slot
+// constants, branch states): the context's set-aside grows to cover it (up
+// to the device's limit; a per-context limit, released with the context),
+// and the special-cell kernels are launched with the window.  WAVEY_L2_PERSIST=0
+// leaves L2 alone.
+void set_l2_window(wavey_cuda_plan *pl) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    pl->l2_window = {};
+    if (!env_int("WAVEY_L2_PERSIST", 1, 0, 1) || ctx->max_persist_l2 <= 0 || ctx->max_window <= 0 || !pl->l2_block_bytes)
+        return;
+    const size_t want = std::min(pl->l2_block_bytes, (size_t)ctx->max_persist_l2);
+    if (want > ctx->persist_set) {
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        ctx->persist_set = want;
+    }
+    const size_t window = std::min(pl->l2_block_bytes, (size_t)ctx->max_window);
+    pl->l2_window.base_ptr = pl->l2_block;
+    pl->l2_window.num_bytes = window;
+    pl->l2_window.hitRatio = (float)std::min(1.0, (double)ctx->persist_set / (double)window);
+    pl->l2_window.hitProp = cudaAccessPropertyPersisting;
+    pl->l2_window.missProp = cudaAccessPropertyStreaming;
+}
+
+// The special list ordered by (tile, plane) for tiles of `rows` rows, as the
+// fused form reads it (wk::SpecTile): a stable counting sort of the records
+// (in cell order) by the key (tile row, tile column, z), and the first record
+// of every key.  Built once per tile height.
+int tile_specials(wavey_cuda_plan *pl, int rows) {
+    const int slot = tile_slot(rows);
+    if (pl->sp_tile[slot]) return WAVEY_OK;
+    const int64_t cells_row = wk::TMA_ROW_FLOATS / pl->V;
+    const int64_t tiles_x = (pl->nx + cells_row - 1) / cells_row, tiles_y = (pl->ny - 2 + rows - 1) / rows;
+    const int64_t keys = tiles_x * tiles_y * pl->nz;
+    const int64_t nxy = pl->nxp * pl->ny;
+    if (keys >= (int64_t)UINT32_MAX) return pl->ctx->fail(WAVEY_E_LIMIT, "too many tiles for the special-cell order");
+    std::vector<uint32_t> off((size_t)keys + 1, 0u), key(pl->sp_host.size());
+    for (size_t i = 0; i < pl->sp_host.size(); i++) {
+        const int64_t cell = pl->sp_host[i].x;
+        const int64_t z = cell / nxy, y = (cell % nxy) / pl->nxp, x = cell % pl->nxp;
+        key[i] = (uint32_t)((((y - 1) / rows) * tiles_x + x / cells_row) * pl->nz + z);
+        off[key[i] + 1]++;
+    }
+    for (int64_t k = 0; k < keys; k++) off[k + 1] += off[k];
+    std::vector<uint32_t> pos(off.begin(), off.end() - 1);
+    std::vector<uint4> rec(pl->sp_host.size());
+    for (size_t i = 0; i < pl->sp_host.size(); i++) rec[pos[key[i]]++] = pl->sp_host[i];
+    int st = upload(pl, &pl->sp_tile[slot], rec.data(), rec.size() * sizeof(uint4));
+    if (!st) st = upload(pl, &pl->sp_off[slot], off.data(), off.size() * sizeof(uint32_t));
+    // The staging vectors die here: wait for the copies.
+    if (!st) st = pl->ctx->cuda(cudaStreamSynchronize(pl->ctx->stream), "upload sync");
+    return st;
+}
+
 // Shape of the TMA interior kernel: tile rows and ring depths (TMA_CFGS[cfg])
 // and the z planes each CTA marches (zt).  Encodes the tensor maps, whose
 // boxes depend on the tile rows, and sizes the grid.
@@ -653,7 +768,13 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
         if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS)
             return ctx->fail(WAVEY_E_CUDA, "tensor map encoding failed (%d, %d)", (int)r1, (int)r2);
     }
-    if (half) zt = std::min(zt, wk::TMA_MAX_ZT);  // the FP16 kernel stages a z-run's scales in shared memory
+    // The FP16 kernel stages a z-run's scales in shared memory, the fused form
+    // its special-cell offsets: their z-runs have at most TMA_MAX_ZT planes.
+    if (half || pl->branch == BRANCH_FUSED) zt = std::min(zt, wk::TMA_MAX_ZT);
+    if (pl->branch == BRANCH_FUSED) {
+        const int st = tile_specials(pl, rows);
+        if (st) return st;
+    }
     pl->tma_cfg = cfg;
     pl->tma_zt = zt;
     pl->tma_tiles_x = (int)((nx + (wk::TMA_ROW_FLOATS / V) - 1) / (wk::TMA_ROW_FLOATS / V));
@@ -666,19 +787,19 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
 }
 
 // Resident CTAs per SM of one shape of the TMA interior kernel.
-template <class E, int V>
+template <class E, int V, bool SPEC>
 int tma_occupancy(int cfg) {
     int occ = 0;
     const void *f;
     size_t smem;
     switch (cfg) {
-        case 1: f = (const void *)wk::interior_tma<E, V, 8, 8, 4>, smem = wk::tma_smem_of<E, 8, 8, 4>(); break;
-        case 2: f = (const void *)wk::interior_tma<E, V, 16, 6, 4>, smem = wk::tma_smem_of<E, 16, 6, 4>(); break;
-        case 3: f = (const void *)wk::interior_tma<E, V, 16, 8, 4>, smem = wk::tma_smem_of<E, 16, 8, 4>(); break;
-        case 4: f = (const void *)wk::interior_tma<E, V, 16, 5, 3>, smem = wk::tma_smem_of<E, 16, 5, 3>(); break;
-        case 5: f = (const void *)wk::interior_tma<E, V, 32, 5, 3>, smem = wk::tma_smem_of<E, 32, 5, 3>(); break;
-        case 6: f = (const void *)wk::interior_tma<E, V, 32, 4, 2>, smem = wk::tma_smem_of<E, 32, 4, 2>(); break;
-        default: f = (const void *)wk::interior_tma<E, V, 8, 6, 4>, smem = wk::tma_smem_of<E, 8, 6, 4>(); break;
+        case 1: f = (const void *)wk::interior_tma<E, V, 8, 8, 4, SPEC>, smem = wk::tma_smem_of<E, 8, 8, 4, SPEC>(); break;
+        case 2: f = (const void *)wk::interior_tma<E, V, 16, 6, 4, SPEC>, smem = wk::tma_smem_of<E, 16, 6, 4, SPEC>(); break;
+        case 3: f = (const void *)wk::interior_tma<E, V, 16, 8, 4, SPEC>, smem = wk::tma_smem_of<E, 16, 8, 4, SPEC>(); break;
+        case 4: f = (const void *)wk::interior_tma<E, V, 16, 5, 3, SPEC>, smem = wk::tma_smem_of<E, 16, 5, 3, SPEC>(); break;
+        case 5: f = (const void *)wk::interior_tma<E, V, 32, 5, 3, SPEC>, smem = wk::tma_smem_of<E, 32, 5, 3, SPEC>(); break;
+        case 6: f = (const void *)wk::interior_tma<E, V, 32, 4, 2, SPEC>, smem = wk::tma_smem_of<E, 32, 4, 2, SPEC>(); break;
+        default: f = (const void *)wk::interior_tma<E, V, 8, 6, 4, SPEC>, smem = wk::tma_smem_of<E, 8, 6, 4, SPEC>(); break;
     }
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, 256, smem) != cudaSuccess) {
         cudaGetLastError();
@@ -689,7 +810,12 @@ int tma_occupancy(int cfg) {
 
 template <class E>
 int tma_occupancy_v(int V, int cfg) {
-    return V == 4 ? tma_occupancy<E, 4>(cfg) : V == 2 ? tma_occupancy<E, 2>(cfg) : tma_occupancy<E, 1>(cfg);
+    return V == 4 ? tma_occupancy<E, 4, false>(cfg) : V == 2 ? tma_occupancy<E, 2, false>(cfg) : tma_occupancy<E, 1, false>(cfg);
+}
+
+int tma_occupancy_fused(int V, int cfg) {
+    return V == 4 ? tma_occupancy<float, 4, true>(cfg) : V == 2 ? tma_occupancy<float, 2, true>(cfg)
+                                                               : tma_occupancy<float, 1, true>(cfg);
 }
 
 // The z-run that makes the grid of one shape just fill w waves of resident
@@ -697,7 +823,8 @@ int tma_occupancy_v(int V, int cfg) {
 // last wave idles SMs); 0 if none lies in 4..64 planes.
 int wave_zt(const wavey_cuda_plan *pl, int cfg, int w) {
     const int occ = pl->precision == WAVEY_FP16_STORAGE ? tma_occupancy_v<__half>(pl->V, cfg)
-                                                         : tma_occupancy_v<float>(pl->V, cfg);
+                    : pl->branch == BRANCH_FUSED            ? tma_occupancy_fused(pl->V, cfg)
+                                                            : tma_occupancy_v<float>(pl->V, cfg);
     const int64_t planes = pl->nz - 2, rows = TMA_CFGS[cfg].rows, cells_row = wk::TMA_ROW_FLOATS / pl->V;
     const int64_t layer = ((pl->nx + cells_row - 1) / cells_row) * ((pl->ny - 2 + rows - 1) / rows) * pl->chunks;
     const int64_t slots = (int64_t)occ * pl->ctx->sm_count;
@@ -907,11 +1034,28 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     for (int k = 0; k < 2; k++)
         if ((st = alloc(pl, &pl->field[k], pl->field_bytes))) return bail(st);
     if ((st = upload(pl, &pl->mask, mask.data(), mask.size() * 4))) return bail(st);
+    pl->sp_host.resize(cell_l.size());
+    for (size_t i = 0; i < pl->sp_host.size(); i++) pl->sp_host[i] = make_uint4(cell_l[i], meta_l[i], slot0_l[i], tap_l[i]);
+    // One block: records | slot constants | branch states u | g, each part
+    // 256-byte aligned.
+    const size_t sp_bytes = round_up((int64_t)(pl->sp_host.size() * sizeof(uint4)), 256);
+    const size_t slot_bytes = round_up((int64_t)(nslots * 4 * E), 256);
+    pl->state_bytes = (size_t)pl->chunks * nslots * pl->V * E;
+    const size_t st_bytes = round_up((int64_t)pl->state_bytes, 256);
+    pl->l2_block_bytes = sp_bytes + slot_bytes + 2 * st_bytes;
+    if ((st = alloc(pl, &pl->l2_block, pl->l2_block_bytes))) return bail(st);
     {
-        std::vector<uint4> rec(cell_l.size());
-        for (size_t i = 0; i < rec.size(); i++) rec[i] = make_uint4(cell_l[i], meta_l[i], slot0_l[i], tap_l[i]);
-        if ((st = upload(pl, &pl->sp, rec.data(), rec.size() * sizeof(uint4)))) return bail(st);
+        unsigned char *blk = static_cast<unsigned char *>(pl->l2_block);
+        pl->sp = reinterpret_cast<uint4 *>(blk);
+        pl->slots = blk + sp_bytes;
+        pl->su = blk + sp_bytes + slot_bytes;
+        pl->sg = blk + sp_bytes + slot_bytes + st_bytes;
     }
+    if (!pl->sp_host.empty() &&
+        (st = ctx->cuda(cudaMemcpyAsync(pl->sp, pl->sp_host.data(), pl->sp_host.size() * sizeof(uint4),
+                                        cudaMemcpyHostToDevice, ctx->stream), "upload")))
+        return bail(st);
+    pl->h2d_bytes += (int64_t)(pl->sp_host.size() * sizeof(uint4));
     std::vector<double> slot_v(grid->slots ? grid->slots : (const double *)nullptr,
                                grid->slots ? grid->slots + 4 * nslots : (const double *)nullptr);
     std::vector<double> sig_v;
@@ -931,14 +1075,15 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         recv_p[r] = (uint32_t)((z * ny + y) * pl->nxp + x);
     }
     if (precision == WAVEY_FP64) {
-        if ((st = upload_typed<double>(pl, &pl->slots, slot_v))) return bail(st);
+        if ((st = upload_into<double>(pl, pl->slots, slot_v))) return bail(st);
         if ((st = upload_typed<double>(pl, &pl->tapw, tapw))) return bail(st);
         if ((st = upload_typed<double>(pl, &pl->sig, sig_v))) return bail(st);
     } else {
-        if ((st = upload_typed<float>(pl, &pl->slots, slot_v))) return bail(st);
+        if ((st = upload_into<float>(pl, pl->slots, slot_v))) return bail(st);
         if ((st = upload_typed<float>(pl, &pl->tapw, tapw))) return bail(st);
         if ((st = upload_typed<float>(pl, &pl->sig, sig_v))) return bail(st);
     }
+    set_l2_window(pl);
     if (precision == WAVEY_FP16_STORAGE) {
         std::vector<float> wm((size_t)pl->lanes_total, 0.0f);
         for (size_t s2 = 0; s2 < n_sources; s2++) {
@@ -954,9 +1099,6 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     }
     if ((st = upload(pl, &pl->recv, recv_p.data(), recv_p.size() * 4))) return bail(st);
     if ((st = upload(pl, &pl->freqs, freqs, nf * sizeof(double)))) return bail(st);
-    pl->state_bytes = (size_t)pl->chunks * nslots * pl->V * E;
-    if ((st = alloc(pl, &pl->su, pl->state_bytes))) return bail(st);
-    if ((st = alloc(pl, &pl->sg, pl->state_bytes))) return bail(st);
     if ((st = alloc(pl, &pl->ring, (size_t)pl->chunks * wk::RING * n_recv * pl->V * E))) return bail(st);
     if ((st = alloc(pl, &pl->tw, (size_t)wk::RING * nf * 2 * E))) return bail(st);
     pl->acc_bytes = (size_t)pl->chunks * n_recv * nf * pl->V * 2 * sizeof(double);
@@ -981,12 +1123,12 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 2>() : tma_attrs<float, 2>();
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 4>() : tma_attrs<float, 4>();
         if ((st = ctx->cuda(e, "shared memory attribute"))) return bail(st);
+        cudaDeviceGetStreamPriorityRange(&pl->prio_lo, &pl->prio_hi);
+        pl->branch = env_int("WAVEY_BRANCH", 3, 0, precision == WAVEY_FP32 ? BRANCH_FUSED : BRANCH_FUSED - 1);
         const int cfg = env_int("WAVEY_TMA_CFG", precision == WAVEY_FP16_STORAGE ? 6 : 4, 0, TMA_NCFG - 1);
         const int zw = wave_zt(pl, cfg, 1);
         const int zt1 = zw ? std::max(8, zw) : 16;
         if ((st = tma_shape(pl, cfg, env_int("WAVEY_TMA_ZT", zt1, 1, 4096)))) return bail(st);
-        cudaDeviceGetStreamPriorityRange(&pl->prio_lo, &pl->prio_hi);
-        pl->branch = env_int("WAVEY_BRANCH", 3, 0, 8);
         pl->tma = true;
     }
     if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
@@ -1619,8 +1761,17 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
         for (int zt : tune_zts(pl, cfg))
             if ((st = trial(cfg, zt, branch0))) return st;
     const int cfg1 = best_cfg, zt1 = best_zt;
-    for (int branch = 0; branch < 9; branch++)
+    const int forms = pl->precision == WAVEY_FP32 ? BRANCH_FUSED + 1 : BRANCH_FUSED;
+    for (int branch = 0; branch < forms; branch++)
         if (branch != branch0 && (st = trial(cfg1, zt1, branch))) return st;
+    if (best_branch == BRANCH_FUSED) {
+        // Stage 3: the fused form's own best shape (its CTAs carry the
+        // special cells, so another tile height or z-run may win).
+        pl->branch = BRANCH_FUSED;
+        for (int cfg = 0; cfg < TMA_NCFG; cfg++)
+            for (int zt : tune_zts(pl, cfg))
+                if (!(cfg == cfg1 && zt == zt1) && (st = trial(cfg, zt, BRANCH_FUSED))) return st;
+    }
     pl->branch = best_branch;
     if ((st = tma_shape(pl, best_cfg, best_zt))) return st;
     cudaGraphExecDestroy(pl->graph);
@@ -1666,6 +1817,8 @@ int wavey_cuda_create(int device, wavey_cuda_ctx **out) {
     if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) {
         ctx->sm_count = prop.multiProcessorCount;
         snprintf(ctx->name, sizeof ctx->name, "%s", prop.name);
+        ctx->max_persist_l2 = prop.persistingL2CacheMaxSize;
+        ctx->max_window = prop.accessPolicyMaxWindowSize;
     }
     *out = ctx;
     return WAVEY_OK;
