@@ -203,8 +203,9 @@ void wavey_cuda_grid_free(wavey_device_grid *grid);
 
 /* Autotuner of a plan's step kernels (FP32 plans of at least 256 steps).
  * Stage 1 times every shape of the interior kernel -- tile rows (8, 16 or 32)
- * with ring depths, and z planes per CTA (8, 16, 32 and the runs that fill
- * one to four whole waves of resident CTAs); stage 2 times, with that shape,
+ * with ring depths, and z planes per CTA (8, 16, 32 and the runs that cut
+ * the planes into one to eight equal z-tiles) -- each with special-cell forms
+ * 3 and 8 (below) beside it; stage 2 times, with that shape,
  * every form of the special-cell update: forms 0-8 run it in a concurrent
  * kernel, with its register cap (branch / 3: 1, 3 or 4 blocks per SM) and
  * launch priority (branch % 3: equal, special cells first, interior first);
@@ -215,7 +216,7 @@ void wavey_cuda_grid_free(wavey_device_grid *grid);
  * grid, and the plan keeps the fastest.
  * result (nullable) lists the candidates' step times.  Neither stage changes
  * any arithmetic.  Other plans are left as they are. */
-#define WAVEY_TUNE_MAX 64
+#define WAVEY_TUNE_MAX 256
 typedef struct {
     int32_t cfg, zt, rows, p_planes, q_planes, branch;
     double step_us;

@@ -121,7 +121,7 @@ class WaveyPlanInfo(C.Structure):
     ]
 
 
-WAVEY_TUNE_MAX = 64
+WAVEY_TUNE_MAX = 256
 WAVEY_IR_INTEGRATE = 1
 WAVEY_IR_LUNDEBY = 2
 

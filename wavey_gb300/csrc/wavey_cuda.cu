@@ -835,14 +835,19 @@ int wave_zt(const wavey_cuda_plan *pl, int cfg, int w) {
     return zt >= 4 && zt <= 64 ? zt : 0;
 }
 
-// Candidate z-runs of one shape: 8, 16 and 32 planes, and the runs that
-// fill one to four whole waves.
-std::vector<int> tune_zts(const wavey_cuda_plan *pl, int cfg) {
-    std::vector<int> zts = {8, 16, 32};
-    for (int w = 1; w <= 4; w++) {
-        const int zt = wave_zt(pl, cfg, w);
-        if (zt && std::find(zts.begin(), zts.end(), zt) == zts.end()) zts.push_back(zt);
-    }
+// Candidate z-runs: 8, 16 and 32 planes, and the runs that cut the interior
+// planes into 1 to 8 equal z-tiles (a partial wave of interior CTAs can beat
+// a full one: the special-cell kernel then has room beside them).
+std::vector<int> tune_zts(const wavey_cuda_plan *pl) {
+    const bool capped = pl->precision == WAVEY_FP16_STORAGE || pl->branch == BRANCH_FUSED;
+    const int planes = (int)pl->nz - 2;
+    std::vector<int> zts;
+    auto add = [&](int zt) {
+        if (capped) zt = std::min(zt, wk::TMA_MAX_ZT);
+        if (zt >= 1 && std::find(zts.begin(), zts.end(), zt) == zts.end()) zts.push_back(zt);
+    };
+    for (int zt : {8, 16, 32}) add(zt);
+    for (int k = 1; k <= 8; k++) add((planes + k - 1) / k);
     return zts;
 }
 
@@ -1117,14 +1122,18 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     if (standalone && (precision == WAVEY_FP32 || precision == WAVEY_FP16_STORAGE) && tma_selected()) {
         // Untuned default: 16-row tiles with 5/3-plane rings (FP32) or 32-row
         // tiles with 4/2-plane rings (FP16), the z-run that fills one wave of
-        // resident CTAs, and a special-cell branch capped at three blocks per
-        // SM -- the shapes the autotuner most often picks.
+        // resident CTAs, and beside it the special-cell kernel -- FP32: capped
+        // at four blocks per SM with the interior first, so that one of its
+        // blocks fits on every SM beside two interior CTAs; FP16: three blocks
+        // per SM, equal priority -- the forms the autotuner picks on the
+        // pillar room.
         cudaError_t e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 1>() : tma_attrs<float, 1>();
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 2>() : tma_attrs<float, 2>();
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 4>() : tma_attrs<float, 4>();
         if ((st = ctx->cuda(e, "shared memory attribute"))) return bail(st);
         cudaDeviceGetStreamPriorityRange(&pl->prio_lo, &pl->prio_hi);
-        pl->branch = env_int("WAVEY_BRANCH", 3, 0, precision == WAVEY_FP32 ? BRANCH_FUSED : BRANCH_FUSED - 1);
+        pl->branch = env_int("WAVEY_BRANCH", precision == WAVEY_FP32 ? 8 : 3, 0,
+                             precision == WAVEY_FP32 ? BRANCH_FUSED : BRANCH_FUSED - 1);
         const int cfg = env_int("WAVEY_TMA_CFG", precision == WAVEY_FP16_STORAGE ? 6 : 4, 0, TMA_NCFG - 1);
         const int zw = wave_zt(pl, cfg, 1);
         const int zt1 = zw ? std::max(8, zw) : 16;
@@ -1717,9 +1726,13 @@ int rooms_run(wavey_cuda_rooms *rm, const volatile int32_t *cancel, void (*progr
 
 
 // The autotuner.  Stage 1: every candidate shape of the TMA interior kernel
-// runs two 128-step chunks of this plan's own grid; the fastest step span
-// wins.  Stage 2: with that shape, every form of the special-cell branch.
-// The plan keeps the winner.  Needs a TMA plan with at least 256 steps.
+// (tile rows and ring depths, z-run), each with two forms of the
+// special-cell kernel beside it -- equal priority at three blocks per SM, and
+// interior first at four blocks per SM, which fits beside a partial wave of
+// interior CTAs -- runs two 128-step chunks of this plan's own grid; the
+// fastest step span wins.  Stage 2: with that shape, every other form of the
+// special-cell update.  The plan keeps the winner.  Needs a TMA plan with at
+// least 256 steps.
 int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
     wavey_cuda_ctx *ctx = pl->ctx;
     if (res) *res = wavey_tune_result{};
@@ -1756,20 +1769,24 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
         }
         return WAVEY_OK;
     };
-    const int branch0 = pl->branch;
-    for (int cfg = 0; cfg < TMA_NCFG; cfg++)
-        for (int zt : tune_zts(pl, cfg))
-            if ((st = trial(cfg, zt, branch0))) return st;
-    const int cfg1 = best_cfg, zt1 = best_zt;
+    for (int family : {3, 8}) {
+        pl->branch = family;
+        const std::vector<int> zts = tune_zts(pl);
+        for (int cfg = 0; cfg < TMA_NCFG; cfg++)
+            for (int zt : zts)
+                if ((st = trial(cfg, zt, family))) return st;
+    }
+    const int cfg1 = best_cfg, zt1 = best_zt, br1 = best_branch;
     const int forms = pl->precision == WAVEY_FP32 ? BRANCH_FUSED + 1 : BRANCH_FUSED;
     for (int branch = 0; branch < forms; branch++)
-        if (branch != branch0 && (st = trial(cfg1, zt1, branch))) return st;
+        if (branch != br1 && (st = trial(cfg1, zt1, branch))) return st;
     if (best_branch == BRANCH_FUSED) {
         // Stage 3: the fused form's own best shape (its CTAs carry the
         // special cells, so another tile height or z-run may win).
         pl->branch = BRANCH_FUSED;
+        const std::vector<int> zts = tune_zts(pl);
         for (int cfg = 0; cfg < TMA_NCFG; cfg++)
-            for (int zt : tune_zts(pl, cfg))
+            for (int zt : zts)
                 if (!(cfg == cfg1 && zt == zt1) && (st = trial(cfg, zt, BRANCH_FUSED))) return st;
     }
     pl->branch = best_branch;
