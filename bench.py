@@ -1,4 +1,4 @@
-"""Benchmark of the FDTD wave-solver hot path on one GB300 (or N, as replicas).
+"""Benchmark of the FDTD wave-solver hot path on one GB300 (or N, source-sharded).
 
 Workload (default): room_pillars -- a 20 x 15 x 8 m room with four pillars
 at a 500 Hz crossover (294 x 221 x 119 cells, 7.4 M air), five fitted
@@ -20,6 +20,17 @@ right-hand sides, batched in one launch per time step, FP32.  The fields
             source (read p, read and write the older buffer) / the mean step
             span measured with CUDA events around each chunk's step launches
   plain     the same four right-hand sides run one at a time (S = 1 kernel)
+  rooms_batch      the multi-room configuration (room_small's room with 32
+            speakers plus four shoeboxes in one launch per step) against every
+            right-hand side run alone
+  reference_grid   the same room on the grid the reference's `--fdtd 500`
+            builds by default (15 points per wavelength at 707 Hz, 72 M
+            cells), a bounded prefix of its steps, untuned
+  fp16_storage     FP16 field storage, autotuned, its error against FP64
+
+Multi-GPU (--gpus N under torchrun): room_pillars is source-sharded -- rank r
+runs speaker r's four right-hand sides on its own copy of the grid, with no
+exchange on the data path; other workloads run as replicas.
 
 Other workloads: room_hall (the 376 M-cell hall, 64 right-hand sides, a bounded prefix of its steps),
 rooms_batch (room_small's room with 32 speakers plus four shoeboxes in one launch per step, against every
@@ -257,72 +268,123 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------ many rooms
-def run_rooms(args, rank, world):
-    """The multi-room configuration (workload rooms_batch): room_small's room
-    with 32 speakers plus four shoeboxes, every room with its own right-hand
-    sides, signals and receivers, advanced together in one launch per time
-    step (wavey_cuda_rooms_*), against every right-hand side run alone."""
-    from wavey_gb300 import _build
-
-    _build.build()
-    import torch
-
+def rooms_leg(b, warmup: int, runs: int, plain: bool = True, clocks=None):
+    """The multi-room configuration: room_small's room with 32 speakers plus
+    four shoeboxes, every room with its own right-hand sides, signals and
+    receivers, advanced together in one launch per time step
+    (wavey_cuda_rooms_*), and (plain) every right-hand side run alone in a
+    standalone plan of its own.  Returns the numbers and the timed seconds."""
     from wavey_gb300 import workloads as W
-    from wavey_gb300.backend import FP32, CudaBackend, RoomJob
+    from wavey_gb300.backend import FP32, RoomJob
 
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
     scenes = W.rooms_batch()
     jobs = [RoomJob(sc.grid, sc.sources, sc.signal, sc.receivers, sc.freqs) for sc in scenes]
     updates = sum(sc.grid.air * sc.steps * len(sc.sources) for sc in scenes)
     rhs = sum(len(sc.sources) for sc in scenes)
-    b = CudaBackend(dev)
     p = b.rooms_plan(jobs)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         p.run()
-    barrier(world)
-    torch.cuda.synchronize()
     total_ms = 0.0
-    with ClockSampler(dev) as clocks:
-        for _ in range(args.steps):
-            total_ms += p.run(stats=True)["total_ms"]
-    torch.cuda.synchronize()
-    barrier(world)
-    elapsed = max_over_ranks(total_ms / 1e3, world)
-    value = updates * args.steps * world / elapsed / 1e9
+    for _ in range(runs):
+        total_ms += p.run(stats=True)["total_ms"]
     info = p.info(0)
     steps = max(sc.steps for sc in scenes)
     launches = info["graph_kernels"] * (steps // 128) + (steps % 128 + 2 if steps % 128 else 0)
     p.close()
-    # Every right-hand side alone, one standalone plan each.
     t_plain = 0.0
-    if not args.no_plain:
+    if plain:
         for sc in scenes:
             for src in sc.sources:
                 q = b.plan(sc.grid, [src], sc.signal, sc.receivers, sc.freqs, FP32)
                 q.run()
                 t_plain += q.run(stats=True)["total_ms"] / 1e3
                 q.close()
-    plain = updates / t_plain / 1e9 if t_plain else None
+    value = updates * runs / (total_ms / 1e3) / 1e9
+    plain_v = updates / t_plain / 1e9 if t_plain else None
+    return {
+        "value": value, "unit": UNIT, "per_source": value / rhs,
+        "rooms": len(scenes), "right_hand_sides": rhs, "grids": [list(sc.grid.n) for sc in scenes],
+        "time_steps": steps,
+        "plain": plain_v, "batched_over_plain": None if plain_v is None else value / plain_v,
+        "launches_per_run": int(launches),
+        "note": "small grids (not HBM-bound); batched = all rooms in one launch per step, plain = each "
+                "right-hand side in its own plan",
+    }, total_ms / 1e3
+
+
+def run_rooms(args, rank, world):
+    """The multi-room configuration on its own (workload rooms_batch)."""
+    from wavey_gb300 import _build
+
+    _build.build()
+    import torch
+
+    from wavey_gb300.backend import CudaBackend
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    b = CudaBackend(dev)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(dev) as clocks:
+        leg, secs = rooms_leg(b, args.warmup, args.steps, plain=not args.no_plain)
+    torch.cuda.synchronize()
+    barrier(world)
+    elapsed = max_over_ranks(secs, world)
+    value = leg["value"] * secs * world / elapsed
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": elapsed * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "rooms_batch", "rooms": len(scenes), "right_hand_sides": rhs,
-                       "grids": [list(sc.grid.n) for sc in scenes], "time_steps": steps,
+            "config": {"workload": "rooms_batch", "rooms": leg["rooms"], "right_hand_sides": leg["right_hand_sides"],
+                       "grids": leg["grids"], "time_steps": leg["time_steps"],
                        "l2": "small grids (not HBM-bound); no flush",
                        "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
-            "per_source": value / rhs,
-            "plain": {"value": plain, "batched_over_plain": None if plain is None else value / world / plain},
+            "per_source": value / leg["right_hand_sides"],
+            "plain": {"value": leg["plain"],
+                      "batched_over_plain": None if leg["plain"] is None else value / world / leg["plain"]},
             "roofline": None,
             "e2e": None,
             "cpu_baseline": None,
-            "gpu_launches": int(launches * args.steps),
+            "gpu_launches": int(leg["launches_per_run"] * args.steps),
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)
     b.close()
+
+
+def reference_grid_leg(b, steps_timed: int):
+    """room_pillars on the grid `wavey simulate --fdtd 500` builds by default
+    (15 points per wavelength at f_c sqrt 2, ~72 M cells), FP32, untuned
+    default shape, a bounded prefix of its 1.0 s run timed: the step's
+    throughput does not change along the run."""
+    from wavey_gb300 import workloads as W
+    from wavey_gb300.backend import FP32
+
+    sc = W.room_pillars(seed=2, reference_grid=True)
+    full = sc.steps
+    sig = sc.signal[:steps_timed]
+    g = sc.grid
+    p = b.plan(g, sc.sources, sig, sc.receivers, sc.freqs, FP32)
+    p.run()
+    st = p.run(stats=True)
+    info = p.info()
+    p.close()
+    S = len(sc.sources)
+    value = g.air * steps_timed * S / (st["total_ms"] / 1e3) / 1e9
+    step_s = st["step_ms"] / 1e3 / st["step_launches"]
+    peak, kind = peaks()
+    achieved = BYTES_PER_UPDATE * g.air * S / step_s / 1e9
+    return {"value": value, "unit": UNIT, "per_source": value / S, "grid": list(g.n), "air_cells": g.air,
+            "ppw": 15.0, "grid_fmax_hz": sc.notes["grid_fmax"], "right_hand_sides": S,
+            "steps_timed": f"first {steps_timed} of {full} steps", "step_us": step_s * 1e6,
+            "roofline_frac": achieved / peak, "peak_kind": peak_kind_label(kind), "tma_zt": info["tma_zt"],
+            "tma_depth": info["tma_depth"], "branch": info["branch"], "autotuned": False}
+
+
+def peak_kind_label(kind: str) -> str:
+    return "of measured" if kind == "measured" else "of fallback"
 
 
 # ------------------------------------------------------------------ our arm
@@ -460,6 +522,33 @@ def run_ours(args, rank, world):
                "spectra_worst_rel": float(np.abs(spec32 - spec64).max() / np.abs(spec64).max()),
                "reference": "FP64 GPU run of the same grid (WAVEY_FP64)"}
 
+    # The receiver DFT with FP64 twiddles and FP64 chunk sums (the plan option
+    # WAVEY_DFT_FP64=1), on the same shape: its cost and its effect.
+    dft64 = None
+    if not args.no_dft64 and main_precision == FP32 and world == 1:
+        env = {"WAVEY_DFT_FP64": "1", "WAVEY_TMA_CFG": str(info["tma_depth"]), "WAVEY_TMA_ZT": str(info["tma_zt"]),
+               "WAVEY_BRANCH": str(info["branch"])}
+        saved = {k: os.environ.get(k) for k in env}
+        os.environ.update(env)
+        try:
+            pd = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP32)
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    os.environ.pop(k, None)
+                else:
+                    os.environ[k] = v
+        pd.run()
+        rd = [pd.run(stats=True) for _ in range(2)]
+        assert pd.info()["dft_fp64"] == 1
+        specd = pd.read()
+        pd.close()
+        vd = updates_per_run / (sum(r["total_ms"] for r in rd) / len(rd) / 1e3) / 1e9
+        dft64 = {"value": vd, "unit": UNIT, "cost_vs_fp32_sums": value / vd - 1.0,
+                 "spectra_rel_change": float(np.abs(specd - spec32).max() / np.abs(spec32).max())}
+        if acc is not None:
+            dft64["spectra_worst_rel_vs_fp64"] = float(np.abs(specd - spec64).max() / np.abs(spec64).max())
+
     # Receiver impulse responses against an FP64 GPU run of the same grid
     # (the mixed-precision configuration): every right-hand side at every mic,
     # IR mode, and octave-band levels of the mics' spectra.
@@ -509,16 +598,20 @@ def run_ours(args, rank, world):
         p16 = b.plan(g, scene.sources, scene.signal, scene.receivers, scene.freqs, FP16_STORAGE)
         tuned16 = p16.autotune() if not args.no_autotune else None
         p16.run()
-        st16 = p16.run(stats=True)
+        runs16 = [p16.run(stats=True) for _ in range(2)]
         info16 = p16.info()
         spec16 = p16.read()
         p16.close()
-        fp16 = {"value": updates_per_run / (st16["total_ms"] / 1e3) / 1e9, "unit": UNIT,
+        ms16 = sum(r["total_ms"] for r in runs16) / len(runs16)
+        step16 = sum(r["step_ms"] for r in runs16) / sum(r["step_launches"] for r in runs16)
+        fp16 = {"value": updates_per_run / (ms16 / 1e3) / 1e9, "unit": UNIT,
                 "bytes_per_update": 6,
-                "step_us": 1e3 * st16["step_ms"] / st16["step_launches"],
+                "step_us": 1e3 * step16,
+                "runs_timed": len(runs16),
                 "kernel": ("interior_tma<__half> (TMA-fed z-march over FP16 planes) || fdtd_step_half special/record"
                            if info16["interior_kernel"] else "fdtd_step_half (fused, register-queue z-march)"),
-                "autotuned": None if not tuned16 else {k: tuned16[k] for k in ("rows", "p_planes", "q_planes", "zt")}}
+                "autotuned": None if not tuned16 else {k: tuned16[k] for k in ("rows", "p_planes", "q_planes", "zt",
+                                                                             "branch")}}
         if acc is not None:
             h0 = np.ones(len(scene.freqs), complex)
             t16 = np.stack([to_transfer(spec16[s], scene.signal, g, scene.freqs, W.C_AIR, 1.0, h0) for s in range(S)])
@@ -542,6 +635,15 @@ def run_ours(args, rank, world):
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"1 right-hand side, first {args.sample_steps} steps, all receivers and bins, FP64, "
                          f"{dt:.1f} s of step loop (fields allocated and first touched before the clock starts)"}
+
+    # Config 3 (many rooms in one launch per step) and the reference's own
+    # default --fdtd grid of this room, as extra keys of the same line.
+    rooms = refgrid = None
+    if world == 1 and args.workload == "room_pillars":
+        if not args.no_rooms:
+            rooms, _ = rooms_leg(b, warmup=1, runs=2, plain=not args.no_plain)
+        if not args.no_refgrid:
+            refgrid = reference_grid_leg(b, args.refgrid_steps)
 
     kernels_per_run = info["graph_kernels"] * (scene.steps // 128) + (scene.steps % 128 + 2 if scene.steps % 128 else 0)
     if rank == 0:
@@ -574,6 +676,9 @@ def run_ours(args, rank, world):
             "accuracy": acc,
             "ir_accuracy": ir_acc,
             "fp16_storage": fp16,
+            "dft_fp64": dft64,
+            "rooms_batch": rooms,
+            "reference_grid": refgrid,
             "grid_build": grid_build,
             "cpu_baseline": cpu,
             "gpu_launches": int(kernels_per_run * args.steps),
@@ -600,6 +705,10 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp16"],
                     help="field storage of the main timed leg (fp16: FP16 storage, FP32 arithmetic)")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-rooms", action="store_true", help="leave out the multi-room key (rooms_batch)")
+    ap.add_argument("--no-dft64", action="store_true", help="leave out the FP64-accumulation key (dft_fp64)")
+    ap.add_argument("--no-refgrid", action="store_true", help="leave out the reference-default-grid key")
+    ap.add_argument("--refgrid-steps", type=int, default=384)
     ap.add_argument("--hall-steps", type=int, default=384)
     ap.add_argument("--hall-speakers", type=int, default=16)
     ap.add_argument("--ir-accuracy", action="store_true",

@@ -96,6 +96,10 @@ typedef struct {
                                              2: 16/6/4, 3: 16/8/4, 4: 16/5/3, 5: 32/5/3, 6: 32/4/2
                                              (-1: no TMA kernel) */
     int32_t branch;                       /* form of the special-cell branch beside it (see wavey_tune_result) */
+    int32_t dft_fp64;                     /* 1: receiver DFT with FP64 twiddles and FP64 sums over each 128-step
+                                             chunk (FP64 plans, and FP32 / FP16 plans created with
+                                             WAVEY_DFT_FP64=1 in the environment); 0: FP32 chunk sums added
+                                             into the FP64 spectra */
 } wavey_plan_info;
 
 int wavey_cuda_create(int device, wavey_cuda_ctx **out);

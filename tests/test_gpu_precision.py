@@ -50,3 +50,30 @@ def test_fp64_gpu_matches_oracle_spectra(backend, library):
     ref = ofd.run(g, taps, sig, rcv, freqs, "f64")
     spec = backend.run_batch(g, [taps], sig, rcv, freqs, precision=FP64)
     assert worst_relative(ref, spec[0]) < 1e-9
+
+
+def test_fp64_receiver_accumulation_option(backend):
+    """WAVEY_DFT_FP64=1: FP32 fields with the receiver DFT folded in FP64
+    (FP64 twiddles, FP64 sums over each 128-step chunk).  The time series are
+    the FP32 run's bit for bit (only the fold changes); the spectra stay
+    within the reference's 1e-3 bar of the FP64 oracle and move by no more
+    than FP32 chunk-sum rounding from the FP32-fold spectra."""
+    import os
+
+    from wavey_gb300.backend import FP32
+
+    g, taps, sig, rcv, freqs = spread_source()
+    ref_spec, ref_ir = backend.run_batch(g, [taps], sig, rcv, freqs, precision=FP32, ir=True)
+    os.environ["WAVEY_DFT_FP64"] = "1"
+    try:
+        plan = backend.plan(g, [taps], sig, rcv, freqs, precision=FP32, ir=True)
+        assert plan.info()["dft_fp64"] == 1
+        plan.run()
+        spec, ir = plan.read()
+        plan.close()
+    finally:
+        del os.environ["WAVEY_DFT_FP64"]
+    assert np.array_equal(ir, ref_ir)
+    ora = ofd.run(g, taps, sig, rcv, freqs, "f64")
+    assert worst_relative(ora, spec[0]) < 1e-3
+    assert worst_relative(ref_spec, spec) < 1e-5

@@ -484,9 +484,10 @@ __global__ void twiddle_chunk(const double *freqs, int nf, double dt, const long
 
 // ------------------------------------------------------------------ DFT
 // acc[c][r][f][l] += sum_t ring[c][t][r][l] * tw[t][f], the partial sum of a
-// chunk in T, added into FP64.  One thread per (chunk, receiver, freq).
-template <class T, int V>
-__global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const T *tw, double *acc, int n_recv, int nf, int chunks,
+// chunk in A (the samples' type T, or FP64 for FP64 accumulation of FP32
+// samples), added into FP64.  One thread per (chunk, receiver, freq).
+template <class T, int V, class A = T>
+__global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const A *tw, double *acc, int n_recv, int nf, int chunks,
                                                    int count, const long long *base, long long steps) {
     count = (int)min((long long)count, steps - *base);
     const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
@@ -495,17 +496,17 @@ __global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const T *tw, d
     const long long rf = idx % ((long long)n_recv * nf);
     const int c = (int)(idx / ((long long)n_recv * nf));
     const int r = (int)(rf / nf), f = (int)(rf - (long long)r * nf);
-    T re[V], im[V];
+    A re[V], im[V];
 #pragma unroll
-    for (int l = 0; l < V; l++) re[l] = im[l] = T(0);
+    for (int l = 0; l < V; l++) re[l] = im[l] = A(0);
     const T *src = ring + ((long long)c * RING * n_recv + r) * V;
     for (int t = 0; t < count; t++) {
         const Lanes<T, V> v = load<T, V, true>(src + (long long)t * n_recv * V);
-        const T wr = __ldg(tw + 2 * (t * nf + f)), wi = __ldg(tw + 2 * (t * nf + f) + 1);
+        const A wr = __ldg(tw + 2 * (t * nf + f)), wi = __ldg(tw + 2 * (t * nf + f) + 1);
 #pragma unroll
         for (int l = 0; l < V; l++) {
-            re[l] = fma(v.v[l], wr, re[l]);
-            im[l] = fma(v.v[l], wi, im[l]);
+            re[l] = fma((A)v.v[l], wr, re[l]);
+            im[l] = fma((A)v.v[l], wi, im[l]);
         }
     }
     double *out = acc + idx * V * 2;

@@ -83,7 +83,9 @@ struct wavey_cuda_ctx {
     int sm_count = 0;
     int max_persist_l2 = 0;     // bytes of L2 that may be set aside for persisting accesses
     int max_window = 0;         // largest access-policy window
-    size_t persist_set = 0;     // persisting set-aside requested so far by this context's plans
+    size_t l2_bytes = 0;        // L2 size
+    size_t persist_set = 0;     // persisting set-aside now in force
+    const void *persist_owner = nullptr;  // the plan whose set-aside and lines are in force
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;  // the special-cell branch of a TMA step
     std::mutex mu;
@@ -156,9 +158,11 @@ struct wavey_cuda_plan {
     // block, kept resident in L2 across steps by a persisting access-policy
     // window on the special-cell kernel (the field streams would otherwise
     // evict them every step).
+    bool dft64 = false;  // FP32 / FP16 plans: receiver DFT with FP64 twiddles and chunk sums
     void *l2_block = nullptr;
     size_t l2_block_bytes = 0;
     cudaAccessPolicyWindow l2_window = {};
+    size_t l2_setaside = 0;   // persisting set-aside this plan asks for
     uint4 *sp_tile[3] = {nullptr, nullptr, nullptr};     // per tile height 8, 16, 32: records by (tile, plane)
     uint32_t *sp_off[3] = {nullptr, nullptr, nullptr};   // and the first record of each (tile, plane)
     int prio_lo = 0, prio_hi = 0;
@@ -173,7 +177,10 @@ struct wavey_cuda_plan {
     ~wavey_cuda_plan() {
         if (graph) cudaGraphExecDestroy(graph);
         // Lines of the freed special block would keep their persisting state.
-        if (l2_window.num_bytes) cudaCtxResetPersistingL2Cache();
+        if (ctx && ctx->persist_owner == this) {
+            cudaCtxResetPersistingL2Cache();
+            ctx->persist_owner = nullptr;
+        }
         for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1, inflight[0], inflight[1], inflight[2], inflight[3], ev_fork, ev_join})
             if (e) cudaEventDestroy(e);
         for (DevBuf &b : bufs)
@@ -588,17 +595,19 @@ void step(wavey_cuda_plan *pl, int t, int parity) {
     }
 }
 
-template <class T, int V>
+// A: the type of the twiddles and of the chunk sums (T, or FP64 for FP32
+// samples in a plan with FP64 receiver accumulation).
+template <class T, int V, class A = T>
 void launch_fold(wavey_cuda_plan *pl, int count) {
     cudaStream_t s = pl->ctx->stream;
     const int tw_threads = count * (int)pl->nf;
     if (tw_threads > 0)
-        wk::twiddle_chunk<T><<<(tw_threads + 255) / 256, 256, 0, s>>>(pl->freqs, (int)pl->nf, pl->dt, pl->base, count,
-                                                                       (long long)pl->steps, reinterpret_cast<T *>(pl->tw));
+        wk::twiddle_chunk<A><<<(tw_threads + 255) / 256, 256, 0, s>>>(pl->freqs, (int)pl->nf, pl->dt, pl->base, count,
+                                                                       (long long)pl->steps, reinterpret_cast<A *>(pl->tw));
     const long long total = (long long)pl->chunks * pl->n_recv * pl->nf;
     if (total > 0)
-        wk::dft_chunk<T, V><<<(unsigned)((total + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
-            reinterpret_cast<const T *>(pl->ring), reinterpret_cast<const T *>(pl->tw), pl->acc, (int)pl->n_recv, (int)pl->nf,
+        wk::dft_chunk<T, V, A><<<(unsigned)((total + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
+            reinterpret_cast<const T *>(pl->ring), reinterpret_cast<const A *>(pl->tw), pl->acc, (int)pl->n_recv, (int)pl->nf,
             pl->chunks, count, pl->base, (long long)pl->steps);
     if (pl->want_ir) {
         const long long n = (long long)pl->chunks * V * pl->n_recv * count;
@@ -615,6 +624,12 @@ void fold(wavey_cuda_plan *pl, int count) {
             case 1: launch_fold<double, 1>(pl, count); break;
             case 2: launch_fold<double, 2>(pl, count); break;
             default: launch_fold<double, 4>(pl, count); break;
+        }
+    } else if (pl->dft64) {  // FP32 samples, FP64 twiddles and chunk sums
+        switch (pl->V) {
+            case 1: launch_fold<float, 1, double>(pl, count); break;
+            case 2: launch_fold<float, 2, double>(pl, count); break;
+            default: launch_fold<float, 4, double>(pl, count); break;
         }
     } else {
         switch (pl->V) {
@@ -686,29 +701,44 @@ int upload_into(wavey_cuda_plan *pl, void *dst, const std::vector<double> &src) 
 }
 
 // The persisting L2 window over the plan's special block (records, slot
-// constants, branch states): the context's set-aside grows to cover it (up
-// to the device's limit; a per-context limit, released with the context),
-// and the special-cell kernels are launched with the window.  WAVEY_L2_PERSIST=0
-// leaves L2 alone.
+// constants, branch states), for blocks that fit whole in a set-aside of at
+// most half of L2 (the field streams keep the other half for their halo
+// reuse).  A block that does not fit gets no window: persisting a part of
+// it was measured slower than none (72 M-cell grid: 786 vs 614 us per step).
+// WAVEY_L2_PERSIST=0 leaves L2 alone.
 void set_l2_window(wavey_cuda_plan *pl) {
     wavey_cuda_ctx *ctx = pl->ctx;
     pl->l2_window = {};
+    pl->l2_setaside = 0;
     if (!env_int("WAVEY_L2_PERSIST", 1, 0, 1) || ctx->max_persist_l2 <= 0 || ctx->max_window <= 0 || !pl->l2_block_bytes)
         return;
-    const size_t want = std::min(pl->l2_block_bytes, (size_t)ctx->max_persist_l2);
-    if (want > ctx->persist_set) {
-        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, want) != cudaSuccess) {
-            cudaGetLastError();
-            return;
-        }
-        ctx->persist_set = want;
-    }
-    const size_t window = std::min(pl->l2_block_bytes, (size_t)ctx->max_window);
+    const size_t cap = std::min({(size_t)ctx->max_persist_l2, ctx->l2_bytes / 2, (size_t)ctx->max_window});
+    if (pl->l2_block_bytes > cap) return;
+    pl->l2_setaside = pl->l2_block_bytes;
     pl->l2_window.base_ptr = pl->l2_block;
-    pl->l2_window.num_bytes = window;
-    pl->l2_window.hitRatio = (float)std::min(1.0, (double)ctx->persist_set / (double)window);
+    pl->l2_window.num_bytes = pl->l2_block_bytes;
+    pl->l2_window.hitRatio = 1.0f;
     pl->l2_window.hitProp = cudaAccessPropertyPersisting;
     pl->l2_window.missProp = cudaAccessPropertyStreaming;
+}
+
+// Before a plan runs: the context's persisting set-aside becomes this
+// plan's (a per-context limit, released with the context), and lines left
+// persisting by another plan go back to normal.  A plan without a window
+// gives the whole L2 back to normal lines.
+void apply_l2(wavey_cuda_plan *pl) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    if (ctx->persist_owner == pl) return;
+    if (ctx->persist_set) cudaCtxResetPersistingL2Cache();
+    if (ctx->persist_set != pl->l2_setaside) {
+        if (cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, pl->l2_setaside) == cudaSuccess) {
+            ctx->persist_set = pl->l2_setaside;
+        } else {
+            cudaGetLastError();
+            pl->l2_window = {};  // launch without the window
+        }
+    }
+    ctx->persist_owner = pl;
 }
 
 // The special list ordered by (tile, plane) for tiles of `rows` rows, as the
@@ -1105,7 +1135,8 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     if ((st = upload(pl, &pl->recv, recv_p.data(), recv_p.size() * 4))) return bail(st);
     if ((st = upload(pl, &pl->freqs, freqs, nf * sizeof(double)))) return bail(st);
     if ((st = alloc(pl, &pl->ring, (size_t)pl->chunks * wk::RING * n_recv * pl->V * E))) return bail(st);
-    if ((st = alloc(pl, &pl->tw, (size_t)wk::RING * nf * 2 * E))) return bail(st);
+    pl->dft64 = precision != WAVEY_FP64 && env_int("WAVEY_DFT_FP64", 0, 0, 1);
+    if ((st = alloc(pl, &pl->tw, (size_t)wk::RING * nf * 2 * (pl->dft64 ? sizeof(double) : E)))) return bail(st);
     pl->acc_bytes = (size_t)pl->chunks * n_recv * nf * pl->V * 2 * sizeof(double);
     if ((st = alloc(pl, &pl->acc, pl->acc_bytes))) return bail(st);
     if ((st = alloc(pl, &pl->base, sizeof(long long)))) return bail(st);
@@ -1153,6 +1184,7 @@ int plan_reset(wavey_cuda_plan *pl) {
     wavey_cuda_ctx *ctx = pl->ctx;
     cudaStream_t s = ctx->stream;
     int st;
+    apply_l2(pl);
     for (int k = 0; k < 2; k++)
         if ((st = ctx->cuda(cudaMemsetAsync(pl->field[k], 0, pl->field_bytes, s), "memset"))) return st;
     if (pl->state_bytes) {
@@ -1836,6 +1868,7 @@ int wavey_cuda_create(int device, wavey_cuda_ctx **out) {
         snprintf(ctx->name, sizeof ctx->name, "%s", prop.name);
         ctx->max_persist_l2 = prop.persistingL2CacheMaxSize;
         ctx->max_window = prop.accessPolicyMaxWindowSize;
+        ctx->l2_bytes = (size_t)prop.l2CacheSize;
     }
     *out = ctx;
     return WAVEY_OK;
@@ -1953,6 +1986,7 @@ int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
     info->tma_zt = pl->tma ? pl->tma_zt : 0;
     info->tma_depth = pl->tma ? pl->tma_cfg : -1;
     info->branch = pl->tma ? pl->branch : -1;
+    info->dft_fp64 = pl->precision == WAVEY_FP64 || pl->dft64 ? 1 : 0;
     return WAVEY_OK;
 }
 

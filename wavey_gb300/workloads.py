@@ -122,7 +122,13 @@ def room_small(seed: int = 1) -> Scene:
 
 
 def room_pillars(seed: int = 2, duration: float = 1.0, n_materials: int = 5, plane_spacing: float = 0.25,
-                 n_mics: int = 64) -> Scene:
+                 n_mics: int = 64, reference_grid: bool = False) -> Scene:
+    """reference_grid: the grid `wavey simulate --fdtd 500` builds by default
+    (FdtdSettings::default, fdtd.rs:119-156: 15 points per wavelength at
+    grid_fmax = f_c sqrt 2, 2.12 times finer per axis, ~72 M cells) and the
+    signal band of run.rs:612, instead of the benchmark configurations'
+    ppw-10 rule at f_c; the room, materials, source and receivers are the
+    same."""
     rng = np.random.default_rng(seed)
     fc = 500.0
     pillars = _pillars(rng, 4, 20.0, 15.0)
@@ -130,7 +136,13 @@ def room_pillars(seed: int = 2, duration: float = 1.0, n_materials: int = 5, pla
     mats = _materials(rng, n_materials)
     assign = [mats[int(k)] for k in rng.integers(0, n_materials, room.n_surfaces)]
     fits = fit_surfaces(assign, (20.0, fc * math.sqrt(2.0)))
-    g = FdtdGrid.build(room, fits, C_AIR, fc, 10.0)
+    if reference_grid:
+        settings = FdtdSettings(crossover_hz=fc)
+        f_grid = settings.grid_fmax(wave_freqs(fc))
+        g = FdtdGrid.build(room, fits, C_AIR, f_grid, settings.points_per_wavelength)
+    else:
+        f_grid = fc
+        g = FdtdGrid.build(room, fits, C_AIR, fc, 10.0)
     pos = _random_points(rng, room, 1, margin=2.0)[0]
     yaw, pitch = float(rng.uniform(0, 360)), float(rng.uniform(-30, 30))
     node = g.nearest_air(pos)
@@ -146,10 +158,11 @@ def room_pillars(seed: int = 2, duration: float = 1.0, n_materials: int = 5, pla
     for f in freqs:
         a0, a, _res = fit_first_order(cardioid, rot, f)
         weights.append(component_weights(a0, a, 2.0 * math.pi * f / C_AIR, g.dx))
-    return Scene("room_pillars", room, g, fits, comps, source_signal(fc, g.dt, steps), mics + plane, freqs, fc,
-                 weights=weights,
+    return Scene("room_pillars_reference_grid" if reference_grid else "room_pillars", room, g, fits, comps,
+                 source_signal(f_grid, g.dt, steps), mics + plane, freqs, fc, weights=weights,
                  notes={"seed": seed, "pillars": pillars, "source": pos, "yaw": yaw, "pitch": pitch,
-                        "mics": len(mics), "plane_points": len(plane)})
+                        "mics": len(mics), "plane_points": len(plane), "grid_fmax": f_grid,
+                        "ppw": 15.0 if reference_grid else 10.0})
 
 
 def room_pillars_shard(rank: int, world: int, seed: int = 7) -> Scene:
