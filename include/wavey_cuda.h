@@ -93,8 +93,9 @@ typedef struct {
     int32_t interior_kernel;              /* 1: TMA-fed z-march beside the special-cell kernel; 0: fused step kernel */
     int32_t tma_zt;                       /* z planes per CTA of the TMA kernel */
     int32_t tma_depth;                    /* shape of the TMA kernel, rows/p ring/old ring: 0: 8/6/4, 1: 8/8/4,
-                                             2: 16/6/4, 3: 16/8/4, 4: 16/5/3, 5: 32/5/3, 6: 32/4/2
-                                             (-1: no TMA kernel) */
+                                             2: 16/6/4, 3: 16/8/4, 4: 16/5/3, 5: 32/5/3, 6: 32/4/2; FP32
+                                             plans also 7-13: the same shapes with registers capped for
+                                             three resident CTAs per SM (-1: no TMA kernel) */
     int32_t branch;                       /* form of the special-cell branch beside it (see wavey_tune_result) */
     int32_t dft_fp64;                     /* 1: receiver DFT with FP64 twiddles and FP64 sums over each 128-step
                                              chunk (FP64 plans, and FP32 / FP16 plans created with

@@ -124,3 +124,28 @@ def test_fused_form_on_the_pillar_room(backend):
         del os.environ["WAVEY_BRANCH"]
     assert np.array_equal(got[1], ref[1])
     assert np.array_equal(got[0], ref[0])
+
+
+@pytest.mark.parametrize("cfg", range(7, 14))
+def test_fp32_shapes_with_capped_registers_agree(backend, library, cfg):
+    """FP32 shapes 7-13 (the shapes of 0-6 compiled for three resident CTAs
+    per SM) give the register-queue kernel's results bit for bit."""
+    g, taps, sig, rcv, freqs = branch_room(library, 0.1)
+    sources = directional_components(g, (1.6, 1.3, 1.1)) + [taps]
+    os.environ["WAVEY_INTERIOR"] = "regq"
+    try:
+        ref = backend.run_batch(g, sources, sig, rcv, freqs, precision=FP32, ir=True)
+    finally:
+        del os.environ["WAVEY_INTERIOR"]
+    for zt in (1, 3, 64):
+        os.environ["WAVEY_TMA_CFG"], os.environ["WAVEY_TMA_ZT"] = str(cfg), str(zt)
+        try:
+            plan = backend.plan(g, sources, sig, rcv, freqs, precision=FP32, ir=True)
+            assert (plan.info()["tma_depth"], plan.info()["tma_zt"]) == (cfg, zt)
+            plan.run()
+            spec, ir = plan.read()
+            plan.close()
+        finally:
+            del os.environ["WAVEY_TMA_CFG"], os.environ["WAVEY_TMA_ZT"]
+        assert np.array_equal(ir, ref[1]), (cfg, zt)
+        assert np.array_equal(spec, ref[0]), (cfg, zt)

@@ -292,13 +292,14 @@ __host__ __device__ constexpr uint32_t tma_smem_of() {
     return NP * tma_p_stride<E, R>() + NQ * tma_q_bytes<E, R>() + 256 + tma_scale_bytes<E, SPEC>() + 128;
 }
 
-// Registers: the FP32 kernel is compiled for one resident CTA at least
-// (ptxas then gives the 16-row shape 90 registers: two CTAs per SM, which
-// leaves room on every SM for a block of the special-cell kernel beside
-// them -- the fastest arrangement measured); the FP16 kernel, instruction-
-// bound, keeps the compiler's own choice; SPEC caps at three CTAs per SM.
-template <class E, int V, int R, int NP, int NQ, bool SPEC = false>
-__global__ void __launch_bounds__(256, SPEC ? 3 : (sizeof(E) == 2 ? 0 : 1)) interior_tma(const __grid_constant__ CUtensorMap tm_p,
+// Registers (LB: the launch bounds' minimum resident CTAs per SM): FP32
+// kernels come in two policies, LB = 1 (ptxas gives the 16-row shape 90
+// registers: two CTAs per SM, with room on every SM for a block of the
+// special-cell kernel beside them) and LB = 3 (three CTAs per SM, more bytes
+// in flight where the interior dominates); the FP16 kernel, instruction-
+// bound, uses LB = 0, the compiler's own choice; SPEC caps at three CTAs.
+template <class E, int V, int R, int NP, int NQ, bool SPEC = false, int LB = 1>
+__global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_constant__ CUtensorMap tm_p,
                                                     const __grid_constant__ CUtensorMap tm_q, TmaArgs<E> a,
                                                     const __grid_constant__ SpecTile sp) {
     static_assert(!SPEC || sizeof(E) == 4, "special cells inside the march: FP32 fields only");

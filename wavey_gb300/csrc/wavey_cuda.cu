@@ -319,12 +319,20 @@ void launch_step(wavey_cuda_plan *pl, int t, int parity) {
     if (blocks > 0) wk::fdtd_step<T, V, RUST><<<blocks, wk::BLOCK, 0, pl->ctx->stream>>>(a, t);
 }
 
-// Shapes of the TMA interior kernel: rows per tile and ring depths.
+// Shapes of the TMA interior kernel: rows per tile, ring depths and the
+// register policy of FP32 kernels (the launch bounds' minimum resident CTAs:
+// 1 lets ptxas take up to 90 registers in the 16-row shapes, two CTAs per SM
+// with room for a special-cell block beside them; 3 caps them for three CTAs
+// per SM and more bytes in flight).  Shapes 7-13 are 0-6 with the second
+// policy; FP16 and fused (SPEC) kernels have one policy, shapes 0-6.
 struct TmaCfg {
-    int rows, np, nq;
+    int rows, np, nq, lb;
 };
-constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4}, {8, 8, 4}, {16, 6, 4}, {16, 8, 4}, {16, 5, 3}, {32, 5, 3}, {32, 4, 2}};
-constexpr int TMA_NCFG = 7;
+constexpr TmaCfg TMA_CFGS[] = {{8, 6, 4, 1},  {8, 8, 4, 1},  {16, 6, 4, 1}, {16, 8, 4, 1}, {16, 5, 3, 1},
+                               {32, 5, 3, 1}, {32, 4, 2, 1}, {8, 6, 4, 3},  {8, 8, 4, 3},  {16, 6, 4, 3},
+                               {16, 8, 4, 3}, {16, 5, 3, 3}, {32, 5, 3, 3}, {32, 4, 2, 3}};
+constexpr int TMA_NCFG = 14;
+constexpr int TMA_NCFG_ONE_POLICY = 7;
 // Special-cell form in which the interior CTAs update the special cells of
 // their tiles (FP32 plans); forms 0-8 run them in a concurrent kernel.
 constexpr int BRANCH_FUSED = 9;
@@ -332,58 +340,78 @@ constexpr int BRANCH_FUSED = 9;
 // Index of a tile height (8, 16 or 32 rows) in the plan's tile-ordered special lists.
 inline int tile_slot(int rows) { return rows == 8 ? 0 : rows == 16 ? 1 : 2; }
 
-template <class E, int V, int R, int NP, int NQ, bool SPEC>
-void launch_tma(int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
-                const wk::TmaArgs<E> &ta, const wk::SpecTile &sp) {
+// One instantiation of the TMA kernel: its entry and dynamic shared memory.
+struct TmaKernel {
+    const void *fn;
+    uint32_t smem;
+};
+
+template <class E, int V, int R, int NP, int NQ, bool SPEC, int LB>
+TmaKernel tma_kernel_of() {
+    return {(const void *)wk::interior_tma<E, V, R, NP, NQ, SPEC, LB>, wk::tma_smem_of<E, R, NP, NQ, SPEC>()};
+}
+
+// The kernel of shape cfg (TMA_CFGS).  FP16 and fused kernels have one
+// register policy: their shapes 7-13 are shapes 0-6.
+template <class E, int V, bool SPEC>
+TmaKernel tma_kernel(int cfg) {
+    constexpr bool two_policies = sizeof(E) == 4 && !SPEC;
+    constexpr int L1 = sizeof(E) == 2 ? 0 : 1;
+    if constexpr (two_policies) {
+        switch (cfg) {
+            case 7: return tma_kernel_of<E, V, 8, 6, 4, SPEC, 3>();
+            case 8: return tma_kernel_of<E, V, 8, 8, 4, SPEC, 3>();
+            case 9: return tma_kernel_of<E, V, 16, 6, 4, SPEC, 3>();
+            case 10: return tma_kernel_of<E, V, 16, 8, 4, SPEC, 3>();
+            case 11: return tma_kernel_of<E, V, 16, 5, 3, SPEC, 3>();
+            case 12: return tma_kernel_of<E, V, 32, 5, 3, SPEC, 3>();
+            case 13: return tma_kernel_of<E, V, 32, 4, 2, SPEC, 3>();
+            default: break;
+        }
+    }
+    switch (cfg % TMA_NCFG_ONE_POLICY) {
+        case 1: return tma_kernel_of<E, V, 8, 8, 4, SPEC, L1>();
+        case 2: return tma_kernel_of<E, V, 16, 6, 4, SPEC, L1>();
+        case 3: return tma_kernel_of<E, V, 16, 8, 4, SPEC, L1>();
+        case 4: return tma_kernel_of<E, V, 16, 5, 3, SPEC, L1>();
+        case 5: return tma_kernel_of<E, V, 32, 5, 3, SPEC, L1>();
+        case 6: return tma_kernel_of<E, V, 32, 4, 2, SPEC, L1>();
+        default: return tma_kernel_of<E, V, 8, 6, 4, SPEC, L1>();
+    }
+}
+
+template <class E, int V, bool SPEC>
+void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
+                    const wk::TmaArgs<E> &ta, const wk::SpecTile &sp) {
+    const TmaKernel k = tma_kernel<E, V, SPEC>(cfg);
     cudaLaunchConfig_t lc = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributePriority;
     attr[0].val.priority = prio;
     lc.gridDim = dim3(blocks);
     lc.blockDim = dim3(256);
-    lc.dynamicSmemBytes = wk::tma_smem_of<E, R, NP, NQ, SPEC>();
+    lc.dynamicSmemBytes = k.smem;
     lc.stream = s;
     lc.attrs = attr;
     lc.numAttrs = 1;
-    cudaLaunchKernelEx(&lc, wk::interior_tma<E, V, R, NP, NQ, SPEC>, p, q, ta, sp);
-}
-
-template <class E, int V, bool SPEC>
-void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
-                    const wk::TmaArgs<E> &ta, const wk::SpecTile &sp) {
-    switch (cfg) {
-        case 1: launch_tma<E, V, 8, 8, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
-        case 2: launch_tma<E, V, 16, 6, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
-        case 3: launch_tma<E, V, 16, 8, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
-        case 4: launch_tma<E, V, 16, 5, 3, SPEC>(blocks, s, prio, p, q, ta, sp); break;
-        case 5: launch_tma<E, V, 32, 5, 3, SPEC>(blocks, s, prio, p, q, ta, sp); break;
-        case 6: launch_tma<E, V, 32, 4, 2, SPEC>(blocks, s, prio, p, q, ta, sp); break;
-        default: launch_tma<E, V, 8, 6, 4, SPEC>(blocks, s, prio, p, q, ta, sp); break;
-    }
-}
-
-template <class E, int V, int R, int NP, int NQ, bool SPEC>
-cudaError_t tma_attr() {
-    return cudaFuncSetAttribute((const void *)wk::interior_tma<E, V, R, NP, NQ, SPEC>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wk::tma_smem_of<E, R, NP, NQ, SPEC>());
-}
-
-template <class E, int V, bool SPEC>
-cudaError_t tma_attrs_spec() {
-    cudaError_t e[] = {tma_attr<E, V, 8, 6, 4, SPEC>(),  tma_attr<E, V, 8, 8, 4, SPEC>(),  tma_attr<E, V, 16, 6, 4, SPEC>(),
-                       tma_attr<E, V, 16, 8, 4, SPEC>(), tma_attr<E, V, 16, 5, 3, SPEC>(), tma_attr<E, V, 32, 5, 3, SPEC>(),
-                       tma_attr<E, V, 32, 4, 2, SPEC>()};
-    for (cudaError_t x : e)
-        if (x != cudaSuccess) return x;
-    return cudaSuccess;
+    void *args[] = {const_cast<CUtensorMap *>(&p), const_cast<CUtensorMap *>(&q), const_cast<wk::TmaArgs<E> *>(&ta),
+                    const_cast<wk::SpecTile *>(&sp)};
+    cudaLaunchKernelExC(&lc, k.fn, args);
 }
 
 template <class E, int V>
 cudaError_t tma_attrs() {
-    cudaError_t e = tma_attrs_spec<E, V, false>();
-    if constexpr (sizeof(E) == 4)
-        if (e == cudaSuccess) e = tma_attrs_spec<E, V, true>();
-    return e;
+    for (int cfg = 0; cfg < TMA_NCFG; cfg++) {
+        const TmaKernel k = tma_kernel<E, V, false>(cfg);
+        cudaError_t e = cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem);
+        if (e != cudaSuccess) return e;
+        if constexpr (sizeof(E) == 4) {
+            const TmaKernel f = tma_kernel<E, V, true>(cfg);
+            e = cudaFuncSetAttribute(f.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)f.smem);
+            if (e != cudaSuccess) return e;
+        }
+    }
+    return cudaSuccess;
 }
 
 // The TMA kernel's arguments for one step (FP16 fields are unused in FP32).
@@ -820,18 +848,8 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
 template <class E, int V, bool SPEC>
 int tma_occupancy(int cfg) {
     int occ = 0;
-    const void *f;
-    size_t smem;
-    switch (cfg) {
-        case 1: f = (const void *)wk::interior_tma<E, V, 8, 8, 4, SPEC>, smem = wk::tma_smem_of<E, 8, 8, 4, SPEC>(); break;
-        case 2: f = (const void *)wk::interior_tma<E, V, 16, 6, 4, SPEC>, smem = wk::tma_smem_of<E, 16, 6, 4, SPEC>(); break;
-        case 3: f = (const void *)wk::interior_tma<E, V, 16, 8, 4, SPEC>, smem = wk::tma_smem_of<E, 16, 8, 4, SPEC>(); break;
-        case 4: f = (const void *)wk::interior_tma<E, V, 16, 5, 3, SPEC>, smem = wk::tma_smem_of<E, 16, 5, 3, SPEC>(); break;
-        case 5: f = (const void *)wk::interior_tma<E, V, 32, 5, 3, SPEC>, smem = wk::tma_smem_of<E, 32, 5, 3, SPEC>(); break;
-        case 6: f = (const void *)wk::interior_tma<E, V, 32, 4, 2, SPEC>, smem = wk::tma_smem_of<E, 32, 4, 2, SPEC>(); break;
-        default: f = (const void *)wk::interior_tma<E, V, 8, 6, 4, SPEC>, smem = wk::tma_smem_of<E, 8, 6, 4, SPEC>(); break;
-    }
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, 256, smem) != cudaSuccess) {
+    const TmaKernel k = tma_kernel<E, V, SPEC>(cfg);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k.fn, 256, k.smem) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
@@ -846,6 +864,12 @@ int tma_occupancy_v(int V, int cfg) {
 int tma_occupancy_fused(int V, int cfg) {
     return V == 4 ? tma_occupancy<float, 4, true>(cfg) : V == 2 ? tma_occupancy<float, 2, true>(cfg)
                                                                : tma_occupancy<float, 1, true>(cfg);
+}
+
+// Shapes a plan may take: 14 for FP32 plans with a concurrent special-cell
+// kernel, 7 for FP16 and fused plans.
+int tma_ncfg(const wavey_cuda_plan *pl) {
+    return pl->precision == WAVEY_FP32 && pl->branch != BRANCH_FUSED ? TMA_NCFG : TMA_NCFG_ONE_POLICY;
 }
 
 // The z-run that makes the grid of one shape just fill w waves of resident
@@ -1163,9 +1187,22 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 4>() : tma_attrs<float, 4>();
         if ((st = ctx->cuda(e, "shared memory attribute"))) return bail(st);
         cudaDeviceGetStreamPriorityRange(&pl->prio_lo, &pl->prio_hi);
-        pl->branch = env_int("WAVEY_BRANCH", precision == WAVEY_FP32 ? 8 : 3, 0,
+        // FP32: where one z-layer of 16-row interior tiles (all chunks) fills
+        // less than two waves of two CTAs per SM, the interior runs in a
+        // partial wave with a special-cell block beside its CTAs (shape 4,
+        // form 8); where it spans many waves (the 376 M-cell hall), the
+        // three-CTA register policy and equal priority keep more bytes in
+        // flight (shape 11, form 3).
+        bool many_waves = false;
+        if (precision == WAVEY_FP32) {
+            const int64_t cells_row = wk::TMA_ROW_FLOATS / pl->V;
+            const int64_t layer = ((nx + cells_row - 1) / cells_row) * ((ny - 2 + 15) / 16) * pl->chunks;
+            many_waves = layer >= 2 * 2 * (int64_t)ctx->sm_count;
+        }
+        pl->branch = env_int("WAVEY_BRANCH", precision == WAVEY_FP32 ? (many_waves ? 3 : 8) : 3, 0,
                              precision == WAVEY_FP32 ? BRANCH_FUSED : BRANCH_FUSED - 1);
-        const int cfg = env_int("WAVEY_TMA_CFG", precision == WAVEY_FP16_STORAGE ? 6 : 4, 0, TMA_NCFG - 1);
+        const int cfg = env_int("WAVEY_TMA_CFG", precision == WAVEY_FP16_STORAGE ? 6 : (many_waves ? 11 : 4), 0,
+                                tma_ncfg(pl) - 1);
         const int zw = wave_zt(pl, cfg, 1);
         const int zt1 = zw ? std::max(8, zw) : 16;
         if ((st = tma_shape(pl, cfg, env_int("WAVEY_TMA_ZT", zt1, 1, 4096)))) return bail(st);
@@ -1804,7 +1841,7 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
     for (int family : {3, 8}) {
         pl->branch = family;
         const std::vector<int> zts = tune_zts(pl);
-        for (int cfg = 0; cfg < TMA_NCFG; cfg++)
+        for (int cfg = 0; cfg < tma_ncfg(pl); cfg++)
             for (int zt : zts)
                 if ((st = trial(cfg, zt, family))) return st;
     }
@@ -1817,7 +1854,7 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
         // special cells, so another tile height or z-run may win).
         pl->branch = BRANCH_FUSED;
         const std::vector<int> zts = tune_zts(pl);
-        for (int cfg = 0; cfg < TMA_NCFG; cfg++)
+        for (int cfg = 0; cfg < tma_ncfg(pl); cfg++)
             for (int zt : zts)
                 if (!(cfg == cfg1 && zt == zt1) && (st = trial(cfg, zt, BRANCH_FUSED))) return st;
     }
