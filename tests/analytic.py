@@ -220,3 +220,78 @@ def directional_source_reproduces_directivity(run_batch):
             worst = max(worst, abs(measured - fit))
     assert worst < 0.05, f"cardioid: {worst}"
     return worst
+
+
+def spherical_reflection(zeta: complex, cos: float, k: float, r: float) -> complex:
+    """Reflection factor of a point source off a locally reacting plane of
+    normalised impedance zeta (Weyl-van der Pol; reflection.rs:71-82), in
+    the solver's e^{jwt} convention: Q = R + (1 - R) F(w) with
+    F(w) = 1 + j sqrt(pi) w wofz(w) and the numerical distance
+    w = (1 + j)/2 sqrt(k r) (cos + 1/zeta), written in the literature's
+    e^{-iwt} convention (conjugated impedance, conjugated result).  wofz is
+    the Faddeeva function w(z) = e^{-z^2} erfc(-iz) (scipy.special)."""
+    from scipy.special import wofz
+
+    cos = min(max(cos, 0.0), 1.0)
+    beta = 1.0 / np.conj(zeta)
+    rp = (cos - beta) / (cos + beta)
+    w = complex(0.5, 0.5) * math.sqrt(k * r) * (cos + beta)
+    f = 1.0 + 1j * math.sqrt(math.pi) * w * wofz(w)
+    return complex(np.conj(rp + (1.0 - rp) * f))
+
+
+def plane_reflection(zeta: complex, cos: float) -> complex:
+    """Plane-wave reflection factor (reflection.rs:84-88)."""
+    zc = zeta * max(cos, 1e-6)
+    return (zc - 1.0) / (zc + 1.0)
+
+
+def oblique_reflection_matches_spherical_wave_theory(run):
+    """fdtd.rs:519-591: a source and receivers 1.2 m above an impedance
+    floor (alpha 0.3; every other surface rigid), incidence 30-75 deg,
+    gated before any other reflection.  The floor-reflected part is
+    isolated with a second run over a rigid floor:
+    Q = (p_imp - p_dir) / (p_rigid - p_dir), the direct sound along a grid
+    axis known analytically (with the scheme's dispersion).  Q must match
+    the point-source reflection off a locally reacting plane for the fitted
+    impedance within |dQ| < 0.05."""
+    room = BoxRoom(20.0, 14.0, 8.0)
+    f_max = 600.0
+    floor = 0  # BoxRoom surface order: floor first
+    freqs = np.array([200.0, 300.0, 450.0])
+
+    def build(alpha):
+        mats = [scalar_material(0.0)] * room.n_surfaces
+        mats[floor] = scalar_material(alpha)
+        fits = fit_surfaces(mats, (20.0, f_max))
+        return FdtdGrid.build(room, fits, c, f_max, 10.0), fits
+
+    g_imp, fits = build(0.3)
+    g_rig, _ = build(0.0)
+    src = g_imp.nearest_air((8.0, 7.0, 1.2))
+    sp = g_imp.pos(src)
+    h = sp[2]  # the floor is at z = 0
+    angles = [30.0, 45.0, 60.0, 70.0, 75.0]
+    rx = [g_imp.nearest_air(sp + np.array([2.0 * h * math.tan(math.radians(a)), 0.0, 0.0])) for a in angles]
+    steps = int(12.0 / c / g_imp.dt)
+    sig = source_signal(f_max, g_imp.dt, steps)
+    h0 = np.ones(len(freqs))
+    p_imp = to_transfer(run(g_imp, [(src, 1.0)], sig, rx, freqs), sig, g_imp, freqs, c, 1.0, h0)
+    p_rig = to_transfer(run(g_rig, [(src, 1.0)], sig, rx, freqs), sig, g_rig, freqs, c, 1.0, h0)
+    worst, rows = 0.0, []
+    for ri, cell in enumerate(rx):
+        d = float(np.linalg.norm(g_imp.pos(cell) - sp))
+        r2 = math.sqrt(d * d + 4.0 * h * h)
+        cos = 2.0 * h / r2
+        for fi, f in enumerate(freqs):
+            k = 2.0 * math.pi * f / c
+            lag = math.radians(FdtdSettings.phase_error_deg_per_m(f, c, g_imp.dx)) * d
+            direct = np.exp(-1j * (k * d + lag)) / d
+            q = (p_imp[ri, fi] - direct) / (p_rig[ri, fi] - direct)
+            zeta = fits[floor].impedance(f)
+            qs = spherical_reflection(zeta, cos, k, r2)
+            err = abs(q - qs)
+            worst = max(worst, err)
+            rows.append((math.degrees(math.acos(cos)), f, abs(q), abs(qs), abs(plane_reflection(zeta, cos)), err))
+    assert worst < 0.05, f"worst |dQ| {worst}: {rows}"
+    return rows

@@ -65,3 +65,7 @@ def test_fp32_boundary_drift_is_the_shader_arithmetic(backend, library):
     _, ref = ofd.run(g, taps, sig, rcv, [], "f32", ir=True)
     _, got = backend.run_fdtd(g, taps, sig, rcv, [], ir=True)
     assert np.array_equal(got, ref)
+
+
+def test_oblique_reflection_matches_spherical_wave_theory(runners):
+    analytic.oblique_reflection_matches_spherical_wave_theory(runners[0])

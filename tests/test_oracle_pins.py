@@ -55,6 +55,26 @@ def test_directional_source_reproduces_directivity():
     analytic.directional_source_reproduces_directivity(run_batch)
 
 
+def test_oblique_reflection_matches_spherical_wave_theory():
+    analytic.oblique_reflection_matches_spherical_wave_theory(run)
+
+
+def test_spherical_reflection_limits():
+    """reflection.rs tests: the Faddeeva values the reference checks, and the
+    spherical factor tending to the plane-wave one far from the source and
+    to 1 at grazing incidence close to it."""
+    from scipy.special import wofz
+
+    assert abs(wofz(1j) - 0.427583576155807) < 1e-12
+    assert abs(wofz(1.0) - complex(0.367879441171442, 0.607157705841394)) < 1e-12
+    assert abs(wofz(2 + 1j) - complex(0.140239581366278, 0.222213440179899)) < 1e-12
+    zeta = complex(3.0, -1.5)
+    far = analytic.spherical_reflection(zeta, 0.8, 50.0, 1e4)
+    assert abs(far - analytic.plane_reflection(zeta, 0.8)) < 1e-3
+    grazing = analytic.spherical_reflection(zeta, 0.0, 1.0, 0.01)
+    assert abs(grazing - 1.0) < 0.2
+
+
 def test_crossover_blend_is_power_complementary():
     """fdtd.rs:593-616"""
     a = 2.0 * np.exp(0.3j)
