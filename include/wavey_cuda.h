@@ -202,6 +202,16 @@ typedef struct {
 } wavey_grid_shape;
 int wavey_cuda_grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int32_t n_fits, double c,
                           double dx, wavey_device_grid **out, wavey_grid_shape *shape);
+/* The same for a room imported as a mesh (FdtdGrid::build_dx's mesh branch:
+ * column_fill, fdtd.rs:385-422, one thread per grid column, and the closest
+ * triangle behind each missing face): positions [n_tri][3][3] and
+ * tri_surface [n_tri] as wh_mesh_room_triangles gives them, optional rigid
+ * boxes solids [n_solids][6], one fit per surface.  Identical to
+ * wh_grid_build_mesh.  WAVEY_E_LIMIT if a grid column crosses the mesh more
+ * than 128 times. */
+int wavey_cuda_grid_build_mesh(wavey_cuda_ctx *ctx, const double *positions, const uint32_t *tri_surface,
+                               int64_t n_tri, const double *solids, int32_t n_solids, const wh_fit *fits, int32_t n_fits,
+                               double c, double dx, wavey_device_grid **out, wavey_grid_shape *shape);
 int wavey_cuda_grid_read(wavey_device_grid *grid, uint8_t *flags, uint32_t *bidx, uint32_t *bcell, uint32_t *bstart,
                          double *slots);
 void wavey_cuda_grid_free(wavey_device_grid *grid);

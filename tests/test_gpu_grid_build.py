@@ -57,3 +57,38 @@ def test_grid_build_limits(backend):
     room = BoxRoom(400.0, 400.0, 100.0)
     with pytest.raises(WaveyError, match="MAX_CELLS"):
         backend.build_grid(room, [AdmittanceFit(0.1)] * 6, C_AIR, 0.05)
+
+
+def test_mesh_room_cr2(backend):
+    """The BRAS room CR2 (an OBJ mesh) at the 700 Hz grid of the reference's
+    bras_wave run: column_fill and the triangle face lookup on the device
+    give the host builder's arrays."""
+    from cr2_scene import cr2_spec
+    from wavey_gb300 import room_ir
+    from wavey_gb300.materials import fit_surfaces
+
+    spec, _, temperature_c = cr2_spec()
+    c = room_ir.speed_of_sound(temperature_c)
+    fits = fit_surfaces(spec.surface_materials, (20.0, 700.0))
+    host = FdtdGrid.build(spec.room, fits, c, 700.0, 10.0)
+    dev = backend.build_grid(spec.room, fits, c, host.dx)
+    _same(host, dev)
+    assert host.air > 1_000_000
+
+
+def test_mesh_room_with_overhang_and_a_cabinet(backend):
+    """A room swept from a stepped profile with an overhanging slab (the
+    reference's column_fill test room), every surface its own material, and
+    a rigid box inside."""
+    from test_mesh_rooms import swept
+    from wavey_gb300.materials import fit_surfaces, scalar_material
+
+    profile = [(0.0, 0.0), (6.0, 0.0), (6.0, 1.0), (10.0, 1.0), (10.0, 4.0), (0.0, 4.0), (0.0, 2.6), (3.0, 2.6),
+               (3.0, 2.2), (0.0, 2.2)]
+    room = swept(profile, [list(range(10))], 5.0)
+    fits = fit_surfaces([scalar_material(0.05 + 0.03 * i) for i in range(room.n_surfaces)], (20.0, 200.0))
+    solids = [(7.0, 2.0, 1.5, 7.6, 2.5, 2.3)]
+    host = FdtdGrid.build_dx(room, fits, 343.0, 0.08, solids=solids)
+    dev = backend.build_grid(room, fits, 343.0, 0.08, solids=solids)
+    _same(host, dev)
+    assert host.n_boundary > 10_000

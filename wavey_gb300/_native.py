@@ -258,6 +258,9 @@ def cuda() -> C.CDLL:
         "wavey_cuda_plan_band_params": (C.c_int, [vp, c_double_p, C.c_int32, C.c_int32, c_double_p, C.c_size_t]),
         "wavey_cuda_grid_build": (C.c_int, [vp, C.POINTER(WhRoom), C.POINTER(WhFit), C.c_int32, C.c_double, C.c_double,
                                             C.POINTER(vp), C.POINTER(WaveyGridShape)]),
+        "wavey_cuda_grid_build_mesh": (C.c_int, [vp, c_double_p, c_uint32_p, C.c_int64, c_double_p, C.c_int32,
+                                                 C.POINTER(WhFit), C.c_int32, C.c_double, C.c_double,
+                                                 C.POINTER(C.c_void_p), C.POINTER(WaveyGridShape)]),
         "wavey_cuda_grid_read": (C.c_int, [vp, C.POINTER(C.c_uint8), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
                                            C.POINTER(C.c_uint32), c_double_p]),
         "wavey_cuda_grid_free": (None, [vp]),

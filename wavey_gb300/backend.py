@@ -160,19 +160,32 @@ class CudaBackend:
             return None
         return (out, irbuf) if ir else out
 
-    def build_grid(self, room, fits, c: float, dx: float):
-        """FdtdGrid.build_dx on the device (wavey_cuda_grid_build): the same
-        arrays as the host builder, returned as an FdtdGrid."""
+    def build_grid(self, room, fits, c: float, dx: float, solids=()):
+        """FdtdGrid.build_dx on the device (wavey_cuda_grid_build, or
+        wavey_cuda_grid_build_mesh for a MeshRoom with optional rigid boxes
+        `solids`): the same arrays as the host builder, returned as an
+        FdtdGrid."""
         from .fdtd import FdtdGrid
 
         if len(fits) != room.n_surfaces:
             raise ValueError(f"{len(fits)} fits for {room.n_surfaces} surfaces")
-        r, keep = room._c()
         arr = (N.WhFit * len(fits))(*[f._c() for f in fits])
         dg, sh = C.c_void_p(), N.WaveyGridShape()
-        with self._lock:
-            self._check(self._lib.wavey_cuda_grid_build(self._h, C.byref(r), arr, len(fits), float(c), float(dx),
-                                                        C.byref(dg), C.byref(sh)))
+        if hasattr(room, "triangles"):  # MeshRoom
+            pos, srf = room.triangles()
+            pos = np.ascontiguousarray(pos, dtype=np.float64)
+            srf = np.ascontiguousarray(srf, dtype=np.uint32)
+            sol = np.ascontiguousarray(np.asarray(solids, dtype=np.float64).reshape(-1, 6))
+            with self._lock:
+                self._check(self._lib.wavey_cuda_grid_build_mesh(
+                    self._h, N.ptr(pos, C.c_double), N.ptr(srf, C.c_uint32), len(srf),
+                    N.ptr(sol, C.c_double) if len(sol) else None, len(sol), arr, len(fits), float(c), float(dx),
+                    C.byref(dg), C.byref(sh)))
+        else:
+            r, keep = room._c()
+            with self._lock:
+                self._check(self._lib.wavey_cuda_grid_build(self._h, C.byref(r), arr, len(fits), float(c), float(dx),
+                                                            C.byref(dg), C.byref(sh)))
         try:
             out = C.c_void_p()
             st = N.host().wh_grid_alloc(sh.n, sh.origin, sh.dx, sh.dt, sh.air_cells, sh.n_boundary, sh.n_slots,

@@ -1,10 +1,13 @@
 // grid_build.cuh -- FdtdGrid::build_dx (core/wavey-solver/src/fdtd.rs:289-378)
 // on the device, for box and prism rooms with pillars, absorbing blocks and
-// rigid solids: the same classification, neighbour flags, face lookup and
-// boundary slots as the host builder (wavey_gb300/csrc/host/grid.cpp), in
-// the same FP64 operations, so the arrays are identical.  Boundary nodes
-// are numbered in cell order by a scan over the cells.
+// rigid solids, and for rooms imported as triangle meshes: the same
+// classification, neighbour flags, face lookup and boundary slots as the
+// host builders (wavey_gb300/csrc/host/grid.cpp, mesh.cpp), in the same FP64
+// operations, so the arrays are identical.  Boundary nodes are numbered in
+// cell order by a scan over the cells.
 //
+//   grid_column_fill  mesh rooms, one thread per (x, y) column: column_fill
+//                  (fdtd.rs:385-422), the crossings of one upward ray
 //   grid_classify  one thread per cell: rigid solid?  air?  (fdtd.rs:308-337)
 //   grid_flags     one thread per cell: air bit and air-neighbour bits (fdtd.rs:349-356)
 //   grid_nodes     one thread per cell: slot count of a boundary node -- the
@@ -24,15 +27,68 @@ struct GbRect {
     double c, lo[3], hi[3];
 };
 
+// Triangles binned by their extent across one axis (for rays along it):
+// cell (i, j) of a nu x nv grid of side h from (u0, v0) lists the triangles,
+// in triangle order, at list[start[j * nu + i] .. start[j * nu + i + 1]).
+struct GbBins {
+    int u, v;
+    double u0, v0, h;
+    long long nu, nv;
+    const uint32_t *start, *list;
+};
+
 struct GbRoom {
     double x0, y0, x1, y1, height;
     int n_pillars, n_blocks, n_solids, n_rects;
     const double *pillars, *blocks, *solids;  // device copies
     const GbRect *rects;
-    const wh_fit *fits;                       // one per rect
+    const wh_fit *fits;                       // one per rect (mesh rooms: one per surface)
     long long nx, ny, nz;
     double origin[3], dx, dt;
+    // Mesh rooms (mesh != 0): triangles {v0, v1 - v0, v2 - v0}, each
+    // triangle's surface, per-axis bins, and column_fill's inside flags.
+    int mesh;
+    long long n_tri;
+    const double *tri;
+    const uint32_t *tri_surface;
+    GbBins bins[3];
+    const uint8_t *inside;
 };
+
+// Moeller-Trumbore, two-sided (wavey-geom bvh.rs:238-259), each operation
+// rounded on its own as the host builder computes it.  e = [v0, e1, e2].
+__device__ __forceinline__ bool gb_ray_triangle(const double o[3], const double d[3], const double *e, double *t) {
+    auto cross = [](const double *a, const double *b, double *out) {
+        out[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(b[1], a[2]));
+        out[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(b[2], a[0]));
+        out[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(b[0], a[1]));
+    };
+    auto dot = [](const double *a, const double *b) {
+        return __dadd_rn(__dadd_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2]));
+    };
+    double p[3], q[3], s[3];
+    cross(d, e + 6, p);
+    const double det = dot(e + 3, p);
+    if (fabs(det) < 1e-14) return false;
+    const double inv = __ddiv_rn(1.0, det);
+    for (int a = 0; a < 3; a++) s[a] = __dsub_rn(o[a], e[a]);
+    const double u = __dmul_rn(dot(s, p), inv);
+    if (!(u >= -1e-10 && u <= 1.0 + 1e-10)) return false;
+    cross(s, e + 3, q);
+    const double v = __dmul_rn(dot(d, q), inv);
+    if (v < -1e-10 || __dadd_rn(u, v) > 1.0 + 1e-10) return false;
+    *t = __dmul_rn(dot(e + 6, q), inv);
+    return true;
+}
+
+// The bin a ray along b's axis through p falls in, or -1.
+__device__ __forceinline__ long long gb_bin(const GbBins &b, const double p[3]) {
+    const double a = p[b.u], c = p[b.v];
+    if (a < b.u0 || c < b.v0) return -1;
+    const long long i = (long long)floor((a - b.u0) / b.h), j = (long long)floor((c - b.v0) / b.h);
+    if (i >= b.nu || j >= b.nv) return -1;
+    return j * b.nu + i;
+}
 
 __device__ __forceinline__ void gb_center(const GbRoom &r, long long x, long long y, long long z, double p[3]) {
     p[0] = __dadd_rn(r.origin[0], __dmul_rn((double)x, r.dx));
@@ -46,6 +102,70 @@ __device__ __forceinline__ bool gb_in_box(const double *b, const double p[3]) {
 
 __device__ __forceinline__ bool gb_in_rect(double x0, double y0, double x1, double y1, double x, double y) {
     return x >= x0 && x < x1 && y >= y0 && y < y1;
+}
+
+constexpr int GB_MAX_CROSSINGS = 128;
+constexpr int GB_ERR_CROSSINGS = 1;
+
+// column_fill (fdtd.rs:385-422): one upward ray per (x, y) column, moved off
+// the cell centres by (0.0001372, 0.0002918) dx, from one cell below the
+// grid; crossings sorted by parameter, a crossing of one surface side at the
+// same height as the previous one (within 1e-9) counted once; a cell is
+// inside after an odd number of crossings below its centre.
+__global__ void __launch_bounds__(256) grid_column_fill(GbRoom r, uint8_t *inside, int *err) {
+    const long long col = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= r.nx * r.ny) return;
+    const long long x = col % r.nx, y = col / r.nx;
+    double cen[3];
+    gb_center(r, x, y, 0, cen);
+    const double start = __dsub_rn(r.origin[2], r.dx);
+    const double o[3] = {__dadd_rn(cen[0], __dmul_rn(0.0001372, r.dx)), __dadd_rn(cen[1], __dmul_rn(0.0002918, r.dx)),
+                         __dadd_rn(start, 0.0)};
+    const double up[3] = {0.0, 0.0, 1.0};
+    double ht[GB_MAX_CROSSINGS];
+    bool hu[GB_MAX_CROSSINGS];
+    int n = 0;
+    const long long b = gb_bin(r.bins[2], o);
+    if (b >= 0) {
+        for (uint32_t k = r.bins[2].start[b]; k < r.bins[2].start[b + 1]; k++) {
+            const uint32_t t = r.bins[2].list[k];
+            const double *e = r.tri + 9 * (long long)t;
+            double th;
+            if (!gb_ray_triangle(o, up, e, &th) || !(th > 0.0)) continue;
+            if (n == GB_MAX_CROSSINGS) {
+                atomicExch(err, GB_ERR_CROSSINGS);
+                return;
+            }
+            // cross(e1, e2).z > 0: the triangle faces up.  Insertion keeps
+            // equal parameters in triangle order (a stable sort).
+            const bool u = __dsub_rn(__dmul_rn(e[3], e[7]), __dmul_rn(e[6], e[4])) > 0.0;
+            int j = n++;
+            while (j > 0 && ht[j - 1] > th) {
+                ht[j] = ht[j - 1];
+                hu[j] = hu[j - 1];
+                j--;
+            }
+            ht[j] = th;
+            hu[j] = u;
+        }
+    }
+    // Crossings of one side at the same height count once.
+    int m = 0;
+    for (int k = 0; k < n; k++) {
+        if (m > 0 && __dsub_rn(ht[k], ht[m - 1]) < 1e-9 && hu[m - 1] == hu[k]) continue;
+        ht[m] = ht[k];
+        hu[m] = hu[k];
+        m++;
+    }
+    int k = 0;
+    const long long nxy = r.nx * r.ny;
+    for (long long z = 0; z < r.nz; z++) {
+        double p[3];
+        gb_center(r, x, y, z, p);
+        const double tz = __dsub_rn(p[2], start);
+        while (k < m && ht[k] < tz) k++;
+        inside[z * nxy + col] = (k % 2 == 1);
+    }
 }
 
 // room.rs:151-157 (strict 0 < z < h and the plan region) minus the blocks.
@@ -71,7 +191,8 @@ __global__ void __launch_bounds__(256) grid_classify(GbRoom r, uint8_t *solid, u
     bool s = false;
     for (int k = 0; k < r.n_solids && !s; k++) s = gb_in_box(r.solids + 6 * k, p);
     solid[i] = s;
-    air[i] = !s && x > 0 && y > 0 && z > 0 && x < r.nx - 1 && y < r.ny - 1 && z < r.nz - 1 && gb_room_contains(r, p);
+    air[i] = !s && x > 0 && y > 0 && z > 0 && x < r.nx - 1 && y < r.ny - 1 && z < r.nz - 1 &&
+             (r.mesh ? r.inside[i] != 0 : gb_room_contains(r, p));
 }
 
 __global__ void __launch_bounds__(256) grid_flags(GbRoom r, const uint8_t *air, uint8_t *flags) {
@@ -111,6 +232,24 @@ __device__ int gb_faces(const GbRoom &r, const uint8_t *solid, long long x, long
         const double sgn = (k & 1) ? 1.0 : -1.0;
         int best = -1;
         double tbest = reach;
+        if (r.mesh) {
+            // The closest triangle along the face direction, 0 < t < 1.5 dx
+            // (fdtd.rs:357-362); the first in triangle order at equal t.
+            const double dir[3] = {axis == 0 ? sgn : 0.0, axis == 1 ? sgn : 0.0, axis == 2 ? sgn : 0.0};
+            const GbBins &bn = r.bins[axis];
+            const long long b = gb_bin(bn, p);
+            if (b >= 0)
+                for (uint32_t j = bn.start[b]; j < bn.start[b + 1]; j++) {
+                    const uint32_t t = bn.list[j];
+                    double th;
+                    if (gb_ray_triangle(p, dir, r.tri + 9 * (long long)t, &th) && th > 0.0 && th < tbest) {
+                        tbest = th;
+                        best = (int)r.tri_surface[t];
+                    }
+                }
+            if (best >= 0) faces[nf++] = best;
+            continue;
+        }
         for (int q = 0; q < r.n_rects; q++) {
             const GbRect &rc = r.rects[q];
             if (rc.axis != axis) continue;

@@ -1483,19 +1483,106 @@ std::vector<wk::GbRect> room_rects_of(const wh_room *r) {
     return s;
 }
 
-int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int32_t n_fits, double c, double dx,
-               wavey_device_grid **out, wavey_grid_shape *shape) {
+// A room given as triangles (wh_mesh_room_triangles' output): positions
+// [n_tri][3][3], wound to their surface's normal, and each one's surface.
+struct MeshIn {
+    const double *pos;
+    const uint32_t *tri_surface;
+    int64_t n_tri;
+};
+
+// Triangles binned across one axis, as the host builder bins them
+// (mesh.cpp, AxisBins): cells of side max(4 dx, extent / 4096) over the
+// padded bounds; a triangle goes to every cell its padded extent touches.
+struct HostBins {
+    wk::GbBins b{};
+    std::vector<uint32_t> start, list;
+};
+
+HostBins bins_for_axis(const MeshIn &m, int axis, const double lo[3], const double hi[3], double dx) {
+    HostBins hb;
+    wk::GbBins &b = hb.b;
+    b.u = (axis + 1) % 3;
+    b.v = (axis + 2) % 3;
+    double ext2 = 0.0;
+    for (int a = 0; a < 3; a++) ext2 += (hi[a] - lo[a]) * (hi[a] - lo[a]);
+    const double pad = 1e-6 * (1.0 + std::sqrt(ext2));
+    b.u0 = lo[b.u] - 2.0 * pad;
+    b.v0 = lo[b.v] - 2.0 * pad;
+    const double eu = hi[b.u] - lo[b.u] + 4.0 * pad, ev = hi[b.v] - lo[b.v] + 4.0 * pad;
+    b.h = std::max(4.0 * dx, std::max(eu, ev) / 4096.0);
+    b.nu = std::max<long long>(1, (long long)std::ceil(eu / b.h));
+    b.nv = std::max<long long>(1, (long long)std::ceil(ev / b.h));
+    auto cu = [&](double a) { return std::min(b.nu - 1, std::max<long long>(0, (long long)std::floor((a - b.u0) / b.h))); };
+    auto cv = [&](double a) { return std::min(b.nv - 1, std::max<long long>(0, (long long)std::floor((a - b.v0) / b.h))); };
+    std::vector<std::vector<uint32_t>> cells((size_t)(b.nu * b.nv));
+    for (int64_t t = 0; t < m.n_tri; t++) {
+        double a0 = INFINITY, a1 = -INFINITY, c0 = INFINITY, c1 = -INFINITY;
+        for (int k = 0; k < 3; k++) {
+            const double *q = m.pos + 9 * t + 3 * k;
+            a0 = std::min(a0, q[b.u]);
+            a1 = std::max(a1, q[b.u]);
+            c0 = std::min(c0, q[b.v]);
+            c1 = std::max(c1, q[b.v]);
+        }
+        for (long long j = cv(c0 - pad); j <= cv(c1 + pad); j++)
+            for (long long i = cu(a0 - pad); i <= cu(a1 + pad); i++) cells[(size_t)(j * b.nu + i)].push_back((uint32_t)t);
+    }
+    hb.start.assign(cells.size() + 1, 0u);
+    for (size_t k = 0; k < cells.size(); k++) hb.start[k + 1] = hb.start[k] + (uint32_t)cells[k].size();
+    hb.list.reserve(hb.start.back());
+    for (const auto &c : cells) hb.list.insert(hb.list.end(), c.begin(), c.end());
+    return hb;
+}
+
+int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const MeshIn *mesh, const double *mesh_solids,
+               int32_t mesh_n_solids, const wh_fit *fits, int32_t n_fits, double c, double dx, wavey_device_grid **out,
+               wavey_grid_shape *shape) {
     if (!out || !shape) return ctx->fail(WAVEY_E_INVALID, "out or shape is null");
     *out = nullptr;
-    if (!room || !(dx > 0.0) || !(c > 0.0) || !(room->height > 0.0) || room->x1 <= room->x0 || room->y1 <= room->y0)
-        return ctx->fail(WAVEY_E_INVALID, "invalid room or spacing");
-    if ((room->n_pillars > 0 && !room->pillars) || (room->n_blocks > 0 && !room->blocks) ||
-        (room->n_solids > 0 && !room->solids) || room->n_pillars < 0 || room->n_blocks < 0 || room->n_solids < 0)
-        return ctx->fail(WAVEY_E_INVALID, "invalid room lists");
-    const std::vector<wk::GbRect> rects = room_rects_of(room);
-    if ((int)rects.size() != n_fits || !fits) return ctx->fail(WAVEY_E_INVALID, "%d fits for %zu surfaces", n_fits, rects.size());
+    std::vector<wk::GbRect> rects;
+    double lo[3], hi[3];
+    std::vector<double> tri;
+    HostBins bins[3];
+    if (mesh) {
+        if (!mesh->pos || !mesh->tri_surface || mesh->n_tri <= 0 || mesh->n_tri >= (1ll << 31) || !(dx > 0.0) ||
+            !(c > 0.0) || mesh_n_solids < 0 || (mesh_n_solids > 0 && !mesh_solids) || !fits || n_fits <= 0)
+            return ctx->fail(WAVEY_E_INVALID, "invalid mesh room or spacing");
+        for (int a = 0; a < 3; a++) lo[a] = INFINITY, hi[a] = -INFINITY;
+        tri.resize((size_t)mesh->n_tri * 9);
+        for (int64_t t = 0; t < mesh->n_tri; t++) {
+            if (mesh->tri_surface[t] >= (uint32_t)n_fits)
+                return ctx->fail(WAVEY_E_INVALID, "triangle %lld: surface %u without a fit", (long long)t,
+                                 mesh->tri_surface[t]);
+            const double *v = mesh->pos + 9 * t;
+            for (int k = 0; k < 3; k++)
+                for (int a = 0; a < 3; a++) {
+                    lo[a] = std::min(lo[a], v[3 * k + a]);
+                    hi[a] = std::max(hi[a], v[3 * k + a]);
+                }
+            for (int a = 0; a < 3; a++) {
+                tri[9 * t + a] = v[a];
+                tri[9 * t + 3 + a] = v[3 + a] - v[a];
+                tri[9 * t + 6 + a] = v[6 + a] - v[a];
+            }
+        }
+        for (int a = 0; a < 3; a++) bins[a] = bins_for_axis(*mesh, a, lo, hi, dx);
+    } else {
+        if (!room || !(dx > 0.0) || !(c > 0.0) || !(room->height > 0.0) || room->x1 <= room->x0 || room->y1 <= room->y0)
+            return ctx->fail(WAVEY_E_INVALID, "invalid room or spacing");
+        if ((room->n_pillars > 0 && !room->pillars) || (room->n_blocks > 0 && !room->blocks) ||
+            (room->n_solids > 0 && !room->solids) || room->n_pillars < 0 || room->n_blocks < 0 || room->n_solids < 0)
+            return ctx->fail(WAVEY_E_INVALID, "invalid room lists");
+        rects = room_rects_of(room);
+        if ((int)rects.size() != n_fits || !fits)
+            return ctx->fail(WAVEY_E_INVALID, "%d fits for %zu surfaces", n_fits, rects.size());
+        lo[0] = room->x0, lo[1] = room->y0, lo[2] = 0.0;
+        hi[0] = room->x1, hi[1] = room->y1, hi[2] = room->height;
+    }
+    const int n_pillars = mesh ? 0 : room->n_pillars, n_blocks = mesh ? 0 : room->n_blocks;
+    const int n_solids = mesh ? mesh_n_solids : room->n_solids;
+    const double *solids = mesh ? mesh_solids : room->solids;
     wavey_grid_shape sh{};
-    const double lo[3] = {room->x0, room->y0, 0.0}, hi[3] = {room->x1, room->y1, room->height};
     sh.dx = dx;
     sh.dt = WAVEY_COURANT * dx / c;
     for (int a = 0; a < 3; a++) {
@@ -1523,10 +1610,21 @@ int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int
     void *d_pill = nullptr, *d_blk = nullptr, *d_sol = nullptr, *d_rects = nullptr, *d_fits = nullptr, *d_solid = nullptr,
          *d_air = nullptr, *d_cnt = nullptr, *d_atot = nullptr, *d_ntot = nullptr, *d_stot = nullptr, *d_grand = nullptr,
          *d_node_at = nullptr, *d_slot_at = nullptr;
+    void *d_tri = nullptr, *d_tsurf = nullptr, *d_inside = nullptr, *d_err = nullptr, *d_bstart[3] = {}, *d_blist[3] = {};
     int st;
-    if ((st = dalloc(&d_pill, sizeof(double) * 4 * room->n_pillars, false)) ||
-        (st = dalloc(&d_blk, sizeof(double) * 6 * room->n_blocks, false)) ||
-        (st = dalloc(&d_sol, sizeof(double) * 6 * room->n_solids, false)) ||
+    if (mesh) {
+        if ((st = dalloc(&d_tri, sizeof(double) * tri.size(), false)) ||
+            (st = dalloc(&d_tsurf, sizeof(uint32_t) * (size_t)mesh->n_tri, false)) ||
+            (st = dalloc(&d_inside, (size_t)cells, false)) || (st = dalloc(&d_err, sizeof(int), false)))
+            return fail(st);
+        for (int a = 0; a < 3; a++)
+            if ((st = dalloc(&d_bstart[a], 4 * bins[a].start.size(), false)) ||
+                (st = dalloc(&d_blist[a], 4 * bins[a].list.size(), false)))
+                return fail(st);
+    }
+    if ((st = dalloc(&d_pill, sizeof(double) * 4 * n_pillars, false)) ||
+        (st = dalloc(&d_blk, sizeof(double) * 6 * n_blocks, false)) ||
+        (st = dalloc(&d_sol, sizeof(double) * 6 * n_solids, false)) ||
         (st = dalloc(&d_rects, sizeof(wk::GbRect) * rects.size(), false)) ||
         (st = dalloc(&d_fits, sizeof(wh_fit) * n_fits, false)) || (st = dalloc(&d_solid, cells, false)) ||
         (st = dalloc(&d_air, cells, false)) || (st = dalloc(&d_cnt, 4 * (size_t)cells, false)) ||
@@ -1535,17 +1633,39 @@ int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int
         (st = dalloc(&d_node_at, 4 * (size_t)cells, false)) || (st = dalloc(&d_slot_at, 8 * (size_t)cells, false)) ||
         (st = dalloc((void **)&g->flags, cells, true)) || (st = dalloc((void **)&g->bidx, 4 * (size_t)cells, true)))
         return fail(st);
-    if (room->n_pillars) cudaMemcpyAsync(d_pill, room->pillars, sizeof(double) * 4 * room->n_pillars, cudaMemcpyHostToDevice, s);
-    if (room->n_blocks) cudaMemcpyAsync(d_blk, room->blocks, sizeof(double) * 6 * room->n_blocks, cudaMemcpyHostToDevice, s);
-    if (room->n_solids) cudaMemcpyAsync(d_sol, room->solids, sizeof(double) * 6 * room->n_solids, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_rects, rects.data(), sizeof(wk::GbRect) * rects.size(), cudaMemcpyHostToDevice, s);
+    if (n_pillars) cudaMemcpyAsync(d_pill, room->pillars, sizeof(double) * 4 * n_pillars, cudaMemcpyHostToDevice, s);
+    if (n_blocks) cudaMemcpyAsync(d_blk, room->blocks, sizeof(double) * 6 * n_blocks, cudaMemcpyHostToDevice, s);
+    if (n_solids) cudaMemcpyAsync(d_sol, solids, sizeof(double) * 6 * n_solids, cudaMemcpyHostToDevice, s);
+    if (!rects.empty()) cudaMemcpyAsync(d_rects, rects.data(), sizeof(wk::GbRect) * rects.size(), cudaMemcpyHostToDevice, s);
+    if (mesh) {
+        cudaMemcpyAsync(d_tri, tri.data(), sizeof(double) * tri.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_tsurf, mesh->tri_surface, sizeof(uint32_t) * (size_t)mesh->n_tri, cudaMemcpyHostToDevice, s);
+        for (int a = 0; a < 3; a++) {
+            cudaMemcpyAsync(d_bstart[a], bins[a].start.data(), 4 * bins[a].start.size(), cudaMemcpyHostToDevice, s);
+            if (!bins[a].list.empty())
+                cudaMemcpyAsync(d_blist[a], bins[a].list.data(), 4 * bins[a].list.size(), cudaMemcpyHostToDevice, s);
+        }
+        cudaMemsetAsync(d_err, 0, sizeof(int), s);
+    }
     cudaMemcpyAsync(d_fits, fits, sizeof(wh_fit) * n_fits, cudaMemcpyHostToDevice, s);
     cudaMemsetAsync(g->flags, 0, cells, s);
     cudaMemsetAsync(g->bidx, 0xFF, 4 * (size_t)cells, s);
-    wk::GbRoom r;
-    r.x0 = room->x0, r.y0 = room->y0, r.x1 = room->x1, r.y1 = room->y1, r.height = room->height;
-    r.n_pillars = room->n_pillars, r.n_blocks = room->n_blocks, r.n_solids = room->n_solids;
+    wk::GbRoom r{};
+    if (!mesh) r.x0 = room->x0, r.y0 = room->y0, r.x1 = room->x1, r.y1 = room->y1, r.height = room->height;
+    r.n_pillars = n_pillars, r.n_blocks = n_blocks, r.n_solids = n_solids;
     r.n_rects = (int)rects.size();
+    r.mesh = mesh ? 1 : 0;
+    if (mesh) {
+        r.n_tri = mesh->n_tri;
+        r.tri = (const double *)d_tri;
+        r.tri_surface = (const uint32_t *)d_tsurf;
+        for (int a = 0; a < 3; a++) {
+            r.bins[a] = bins[a].b;
+            r.bins[a].start = (const uint32_t *)d_bstart[a];
+            r.bins[a].list = (const uint32_t *)d_blist[a];
+        }
+        r.inside = (const uint8_t *)d_inside;
+    }
     r.pillars = (const double *)d_pill, r.blocks = (const double *)d_blk, r.solids = (const double *)d_sol;
     r.rects = (const wk::GbRect *)d_rects;
     r.fits = (const wh_fit *)d_fits;
@@ -1553,6 +1673,16 @@ int grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit *fits, int
     for (int a = 0; a < 3; a++) r.origin[a] = sh.origin[a];
     r.dx = sh.dx, r.dt = sh.dt;
     const unsigned blocks = (unsigned)((cells + 255) / 256);
+    if (mesh) {
+        const long long cols = (long long)sh.n[0] * sh.n[1];
+        wk::grid_column_fill<<<(unsigned)((cols + 255) / 256), 256, 0, s>>>(r, (uint8_t *)d_inside, (int *)d_err);
+        int err = 0;
+        cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if ((st = ctx->cuda(cudaStreamSynchronize(s), "column fill"))) return fail(st);
+        if (err)
+            return fail(ctx->fail(WAVEY_E_LIMIT, "a grid column crosses the mesh more than %d times",
+                                  wk::GB_MAX_CROSSINGS));
+    }
     wk::grid_classify<<<blocks, 256, 0, s>>>(r, (uint8_t *)d_solid, (uint8_t *)d_air);
     wk::grid_flags<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_air, g->flags);
     wk::grid_nodes<<<blocks, 256, 0, s>>>(r, (const uint8_t *)d_solid, g->flags, (uint32_t *)d_cnt, false, nullptr,
@@ -1982,7 +2112,17 @@ int wavey_cuda_grid_build(wavey_cuda_ctx *ctx, const wh_room *room, const wh_fit
     if (!ctx) return WAVEY_E_INVALID;
     std::lock_guard<std::mutex> lock(ctx->mu);
     cudaSetDevice(ctx->device);
-    return grid_build(ctx, room, fits, n_fits, c, dx, out, shape);
+    return grid_build(ctx, room, nullptr, nullptr, 0, fits, n_fits, c, dx, out, shape);
+}
+
+int wavey_cuda_grid_build_mesh(wavey_cuda_ctx *ctx, const double *positions, const uint32_t *tri_surface,
+                               int64_t n_tri, const double *solids, int32_t n_solids, const wh_fit *fits, int32_t n_fits,
+                               double c, double dx, wavey_device_grid **out, wavey_grid_shape *shape) {
+    if (!ctx) return WAVEY_E_INVALID;
+    std::lock_guard<std::mutex> lock(ctx->mu);
+    cudaSetDevice(ctx->device);
+    const MeshIn m{positions, tri_surface, n_tri};
+    return grid_build(ctx, nullptr, &m, solids, n_solids, fits, n_fits, c, dx, out, shape);
 }
 
 int wavey_cuda_grid_read(wavey_device_grid *grid, uint8_t *flags, uint32_t *bidx, uint32_t *bcell, uint32_t *bstart,
