@@ -229,9 +229,11 @@ void wavey_cuda_grid_free(wavey_device_grid *grid);
  * concurrent kernel.  If form 9 wins, stage 3 times every interior shape
  * again with it.  Each candidate runs two 128-step chunks of the plan's own
  * grid, and the plan keeps the fastest.
- * result (nullable) lists the candidates' step times.  Neither stage changes
- * any arithmetic.  Other plans are left as they are. */
-#define WAVEY_TUNE_MAX 256
+ * result (nullable) lists the candidates' step times (every candidate: at
+ * most 14 shapes x 11 z-runs x 2 families, 9 other forms and the fused
+ * form's 154 shapes, 471 in all).  Neither stage changes any arithmetic.
+ * Other plans are left as they are. */
+#define WAVEY_TUNE_MAX 512
 typedef struct {
     int32_t cfg, zt, rows, p_planes, q_planes, branch;
     double step_us;

@@ -78,6 +78,30 @@ def test_every_tma_shape_agrees(backend, library, precision, cfg):
         assert np.array_equal(spec, ref[0]), (cfg, zt)
 
 
+@pytest.mark.parametrize("precision", [FP32, FP16_STORAGE], ids=["fp32", "fp16"])
+@pytest.mark.parametrize("cfg", [0, 4, 6])
+def test_march_direction_does_not_change_results(backend, library, precision, cfg):
+    """The interior kernel marches z upwards on even steps and downwards on
+    odd ones; WAVEY_ZALT=0 keeps every step upwards.  Both give identical
+    receiver series, with z-runs of 1, 3 (the last run ragged) and 64 planes,
+    over an odd number of steps."""
+    g, taps, sig, rcv, freqs = branch_room(library, 0.1)
+    comps = directional_components(g, (1.6, 1.3, 1.1))
+    sources = comps + [taps]
+    sig = sig[:301]
+    for zt in (1, 3, 64):
+        out = []
+        for zalt in ("0", "1"):
+            os.environ.update(WAVEY_TMA_CFG=str(cfg), WAVEY_TMA_ZT=str(zt), WAVEY_ZALT=zalt)
+            try:
+                out.append(backend.run_batch(g, sources, sig, rcv, freqs, precision=precision, ir=True))
+            finally:
+                for k in ("WAVEY_TMA_CFG", "WAVEY_TMA_ZT", "WAVEY_ZALT"):
+                    del os.environ[k]
+        assert np.array_equal(out[0][1], out[1][1]), zt
+        assert np.array_equal(out[0][0], out[1][0]), zt
+
+
 @pytest.mark.parametrize("lanes", [1, 2, 4])
 @pytest.mark.parametrize("cfg", range(7))
 def test_special_cells_inside_the_march_agree(backend, library, lanes, cfg):

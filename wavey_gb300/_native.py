@@ -122,7 +122,7 @@ class WaveyPlanInfo(C.Structure):
     ]
 
 
-WAVEY_TUNE_MAX = 256
+WAVEY_TUNE_MAX = 512
 WAVEY_IR_INTEGRATE = 1
 WAVEY_IR_LUNDEBY = 2
 

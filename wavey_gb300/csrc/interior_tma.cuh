@@ -2,8 +2,11 @@
 //
 // A CTA owns a tile of R rows x 128 floats of one z-run (32 cells of a
 // 4-source chunk, 64 cells of a 2-source chunk or 128 cells of one source)
-// and marches z.  One thread issues cp.async.bulk.tensor loads of whole
-// planes several planes ahead into a ring in shared memory:
+// and marches z, upwards on even steps and downwards on odd ones (TmaArgs::
+// rev), so that a step begins on the planes the previous step touched last:
+// on grids a few times the size of L2 those reads hit in L2.  One thread
+// issues cp.async.bulk.tensor loads of whole planes several planes ahead
+// into a ring in shared memory:
 //
 //   P ring (NP planes): p^n with a one-row halo in y and a 16-byte halo in x
 //                       (box 136 floats x R+2 rows), so the x, y and z
@@ -105,6 +108,7 @@ struct TmaArgs {
     long long cells_p;
     int nxp, ny, nz, nxw;
     int tiles_x, tiles_y, tiles_z, zt;
+    int rev;                   // march z downwards (1) or upwards (0)
     float l2;
     // FP16 storage only: the step (*base + t), slab scales and maxima.
     const long long *base;
@@ -331,6 +335,13 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
     const int Kq = ze - zs;      // output planes
     const int Kp = Kq + 2;       // p planes zs-1 .. ze
     const int cx = tx * TMA_ROW_FLOATS;
+    // March direction.  Upwards the p planes arrive as zs-1, zs, .., ze and
+    // the output planes as zs .. ze-1; downwards as ze, ze-1, .., zs-1 and
+    // ze-1 .. zs.  Alternating it from step to step starts each step on the
+    // planes the previous one touched last, which are still in L2.
+    const int dz = a.rev ? -1 : 1;
+    const int zq0 = a.rev ? ze - 1 : zs;   // first output plane
+    const int zp0 = zq0 - dz;              // first p plane
 
     // FP16: slab scales of the z-run -- p^n of planes zs-1..ze (2^E of level
     // n), p^(n-1) of planes zs..ze-1 (level n-1), the inverse scales of level
@@ -372,13 +383,13 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
         const int k = np_issued++;
         const uint32_t bar = barP + 8 * (k % NP);
         mbar_expect_tx(bar, PB);
-        tma_load_4d(smem_addr(Pbuf) + (k % NP) * PS, &tm_p, cx - HALO, y0 - 1, zs - 1 + k, c, bar);
+        tma_load_4d(smem_addr(Pbuf) + (k % NP) * PS, &tm_p, cx - HALO, y0 - 1, zp0 + dz * k, c, bar);
     };
     auto issue_q = [&]() {
         const int j = nq_issued++;
         const uint32_t bar = barQ + 8 * (j % NQ);
         mbar_expect_tx(bar, QB);
-        tma_load_4d(smem_addr(Qbuf) + (j % NQ) * QB, &tm_q, cx, y0, zs + j, c, bar);
+        tma_load_4d(smem_addr(Qbuf) + (j % NQ) * QB, &tm_q, cx, y0, zq0 + dz * j, c, bar);
     };
     if (threadIdx.x == 0) {
         while (np_issued < NP && np_issued < Kp) issue_p();
@@ -388,15 +399,10 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
     const int x0 = tx * CELLS + lane * (4 / V);
     E *Q = a.nxt + (long long)c * a.cells_p * V;
     const long long nstep = SPEC ? *a.base + a.t : 0;  // SPEC: the step (signals are indexed by it)
-    const long long mstep = (long long)a.ny * a.nxw;
-    // FP16: the maxima slot of level n+1, and the scales of planes j and j+1.
+    const long long mstep = (long long)dz * a.ny * a.nxw;  // mask words of the next plane in march order
+    // FP16: the maxima slot of level n+1.
     unsigned int *amax_new = nullptr;
-    float scm = 1.0f, scc = 1.0f;
-    if constexpr (HALF) {
-        amax_new = a.amax + ((long long)((*a.base + a.t + 1) % AMAX_RING) * a.chunks + c) * a.nz;
-        scm = ssc[0];
-        scc = ssc[1];
-    }
+    if constexpr (HALF) amax_new = a.amax + ((long long)((*a.base + a.t + 1) % AMAX_RING) * a.chunks + c) * a.nz;
     // Rows of this thread: tile rows warp + 8 r (r < RT).  Interior-mask
     // words, four planes ahead, per row.
     bool rok[RT];
@@ -406,7 +412,7 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
     for (int r = 0; r < RT; r++) {
         const int y = y0 + warp + 8 * r;
         rok[r] = y < a.ny - 1 && x0 < a.nxp;
-        mrow[r] = a.interior + ((long long)zs * a.ny + (rok[r] ? y : 1)) * a.nxw + (rok[r] ? (x0 >> 5) : 0);
+        mrow[r] = a.interior + ((long long)zq0 * a.ny + (rok[r] ? y : 1)) * a.nxw + (rok[r] ? (x0 >> 5) : 0);
 #pragma unroll
         for (int d = 0; d < 4; d++) mw[r][d] = (rok[r] && d < Kq) ? __ldg(mrow[r] + d * mstep) : 0u;
     }
@@ -414,7 +420,7 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
     // Planes 0 and 1 of the p ring are waited for once; afterwards each plane
     // j waits only for p plane j + 2 and old plane j.
     bool ok = mbar_wait(barP, 0) && mbar_wait(barP + 8, 0);
-    int bm = 0, bc = 1, bp = 2;      // buffers of p planes j, j+1, j+2
+    int bm = 0, bc = 1, bp = 2;      // buffers of p planes j, j+1, j+2 in march order
     uint32_t php = 0;                // parity of p plane j+2
     int bq = 0;
     uint32_t phq = 0;
@@ -424,21 +430,25 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
             if (np_issued < Kp) issue_p();
             if (nq_issued < Kq) issue_q();
         }
-        const int z = zs + j;
-        float scp = 1.0f, sco = 1.0f, sinv = 1.0f, slim = 0.0f;
+        const int z = zq0 + dz * j;
+        const int iz = z - zs;       // the plane within the z-run
+        float scm = 1.0f, scc = 1.0f, scp = 1.0f, sco = 1.0f, sinv = 1.0f, slim = 0.0f;
         if constexpr (HALF) {
-            scp = ssc[j + 2];
-            sco = ssc[TMA_SCALE_STRIDE + j];
-            sinv = ssc[2 * TMA_SCALE_STRIDE + j];
-            slim = ssc[3 * TMA_SCALE_STRIDE + j];
+            scm = ssc[iz];
+            scc = ssc[iz + 1];
+            scp = ssc[iz + 2];
+            sco = ssc[TMA_SCALE_STRIDE + iz];
+            sinv = ssc[2 * TMA_SCALE_STRIDE + iz];
+            slim = ssc[3 * TMA_SCALE_STRIDE + iz];
         }
         ok = ok && mbar_wait(barP + 8 * bp, php) && mbar_wait(barQ + 8 * bq, phq);
         uint32_t mb = 0;  // FP16: largest |p^(n+1)| stored, as float bits
         if (ok) {
             const E *pc = Pbuf + bc * (PS / sizeof(E));
-            const E *pn = Pbuf + bp * (PS / sizeof(E));
             const E *qo = Qbuf + bq * (QB / sizeof(E));
-            const E *pm = Pbuf + bm * (PS / sizeof(E));
+            // p^n of planes z - 1 and z + 1: behind and ahead in march order.
+            const E *pm = Pbuf + (a.rev ? bp : bm) * (PS / sizeof(E));
+            const E *pn = Pbuf + (a.rev ? bm : bp) * (PS / sizeof(E));
 #pragma unroll
             for (int r = 0; r < RT; r++) {
                 const uint32_t word = mw[r][0];
@@ -511,7 +521,7 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
                 // The tile's special cells of plane z, from the same staged
                 // planes: one thread per (cell, lane), a cell's lanes on
                 // neighbouring threads.
-                const uint32_t k0 = soff[j], tasks = (soff[j + 1] - k0) * V;
+                const uint32_t k0 = soff[iz], tasks = (soff[iz + 1] - k0) * V;
                 for (uint32_t t = threadIdx.x; t < tasks; t += 256) {
                     const uint4 rec = __ldg(sp.rec + k0 + t / V);
                     const int l = (int)(t % V);
@@ -535,8 +545,6 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
                 atomicExch(a.error, ERR_FP16_RANGE);
             mb = __reduce_max_sync(0xffffffffu, mb);
             if (lane == 0) wmax[(j & 1) * 8 + warp] = mb;
-            scm = scc;
-            scc = scp;
         }
         // One barrier per plane: everyone is done with this plane's buffers
         // (thread 0 refills them next), and a lost wait stops the whole CTA.

@@ -151,6 +151,7 @@ struct wavey_cuda_plan {
     CUtensorMap tm_p[2], tm_q[2];  // per parity: p^n of field[parity], old of field[parity^1]
     int tma_tiles_x = 0, tma_tiles_y = 0, tma_tiles_z = 0, tma_zt = 32, tma_blocks = 0;
     int tma_cfg = 0;      // shape of the TMA kernel, an index into TMA_CFGS
+    bool zalt = true;     // alternate the interior's z-march direction from step to step
     int branch = 0;             // special-cell form: branch < 9: a concurrent kernel with register cap
                                 // (branch / 3) and priority (branch % 3); BRANCH_FUSED: inside the interior CTAs
     std::vector<uint4> sp_host;   // special records in cell order (host copy, for the tile orders)
@@ -430,6 +431,7 @@ wk::TmaArgs<E> tma_args(const wavey_cuda_plan *pl, int t, int parity) {
     ta.tiles_y = pl->tma_tiles_y;
     ta.tiles_z = pl->tma_tiles_z;
     ta.zt = pl->tma_zt;
+    ta.rev = pl->zalt ? (parity & 1) : 0;
     ta.l2 = (float)(COURANT * COURANT);
     ta.base = pl->base;
     ta.t = t;
@@ -1206,6 +1208,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         const int zw = wave_zt(pl, cfg, 1);
         const int zt1 = zw ? std::max(8, zw) : 16;
         if ((st = tma_shape(pl, cfg, env_int("WAVEY_TMA_ZT", zt1, 1, 4096)))) return bail(st);
+        pl->zalt = env_int("WAVEY_ZALT", 1, 0, 1) != 0;
         pl->tma = true;
     }
     if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
