@@ -101,6 +101,10 @@ typedef struct {
                                              chunk (FP64 plans, and FP32 / FP16 plans created with
                                              WAVEY_DFT_FP64=1 in the environment); 0: FP32 chunk sums added
                                              into the FP64 spectra */
+    int32_t two_step;                     /* 1: two steps per pass over the fields (FP32, four sources per chunk,
+                                             created with WAVEY_TBLOCK=1): interior_tb2 beside the special-cell
+                                             kernel, then the shell and special cells of the second step */
+    int32_t two_step_rows, two_step_zt;   /* its output rows per tile and z-run */
 } wavey_plan_info;
 
 int wavey_cuda_create(int device, wavey_cuda_ctx **out);

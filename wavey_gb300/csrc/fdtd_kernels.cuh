@@ -112,6 +112,8 @@ template <class T>
 struct StepArgs {
     const T *cur;              // p^n        [chunks][cells_p][V]
     T *nxt;                    // p^{n-1} in, p^{n+1} out
+    T *out;                    // where the special cells' p^{n+1} goes: nxt, or a third buffer when two
+                               // steps share one pass over the fields
     const uint32_t *interior;  // [nz][ny][nxw] one bit per padded cell
     const uint4 *sp;           // [n_special] {padded cell (ascending), meta, first slot, tap row or NO_TAP};
                                // meta: bits 0-5 air-neighbour flags, bits 6-10 slot count
@@ -188,13 +190,14 @@ template <class T, int V>
 struct PlainField {
     static constexpr bool STREAM = false;
     const T *P;
-    T *Q;
+    T *Q;  // p^(n-1)
+    T *O;  // p^(n+1): Q itself, or a separate buffer
     __device__ __forceinline__ Lanes<T, V> p(long long cell, int) const { return load<T, V, true>(P + cell * V); }
     __device__ __forceinline__ Lanes<T, V> nb(long long cell, int, long long off) const {
         return load<T, V, true>(P + (cell + off) * V);
     }
     __device__ __forceinline__ Lanes<T, V> old(long long cell) const { return load<T, V, false>(Q + cell * V); }
-    __device__ __forceinline__ void put(long long cell, const Lanes<T, V> &v) const { store<T, V>(Q + cell * V, v); }
+    __device__ __forceinline__ void put(long long cell, const Lanes<T, V> &v) const { store<T, V>(O + cell * V, v); }
 };
 
 // The special-cell update of chunk c at step n from its record rec, with
@@ -324,7 +327,8 @@ __device__ __forceinline__ void special_cell(const StepArgs<T> &a, long long k, 
     const int c = (int)(k / a.n_special);
     k -= (long long)c * a.n_special;
     const uint4 rec = __ldg(a.sp + k);
-    const PlainField<T, V> f{a.cur + (long long)c * a.cells_p * V, a.nxt + (long long)c * a.cells_p * V};
+    const PlainField<T, V> f{a.cur + (long long)c * a.cells_p * V, a.nxt + (long long)c * a.cells_p * V,
+                             a.out + (long long)c * a.cells_p * V};
     special_core<T, V, RUST_ORDER, SR>(a, f, rec, c, n);
 }
 

@@ -32,6 +32,7 @@
 #include "fdtd_kernels.cuh"
 #include "interior_tma.cuh"
 #include "ir_analysis.cuh"
+#include "tblock.cuh"
 #include "grid_build.cuh"
 
 namespace {
@@ -152,6 +153,15 @@ struct wavey_cuda_plan {
     int tma_tiles_x = 0, tma_tiles_y = 0, tma_tiles_z = 0, tma_zt = 32, tma_blocks = 0;
     int tma_cfg = 0;      // shape of the TMA kernel, an index into TMA_CFGS
     bool zalt = true;     // alternate the interior's z-march direction from step to step
+    // Two steps per pass (FP32, four sources per chunk): two more field
+    // buffers for p^(n+1) and p^(n+2), the deep-cell mask, the shell list and
+    // the pass's tensor maps (per pair parity) and geometry.
+    bool tb2 = false;
+    void *field2[2] = {nullptr, nullptr};
+    uint32_t *deep = nullptr, *shell = nullptr;
+    int64_t n_shell = 0;
+    CUtensorMap tb_p[2], tb_q[2];
+    int tb_cfg = 0, tb_rows = 0, tb_zt = 0, tb_tiles_x = 0, tb_tiles_y = 0, tb_tiles_z = 0, tb_blocks = 0;
     int branch = 0;             // special-cell form: branch < 9: a concurrent kernel with register cap
                                 // (branch / 3) and priority (branch % 3); BRANCH_FUSED: inside the interior CTAs
     std::vector<uint4> sp_host;   // special records in cell order (host copy, for the tile orders)
@@ -279,6 +289,7 @@ template <class T>
 void fill_args(wavey_cuda_plan *pl, wk::StepArgs<T> &a, int parity) {
     a.cur = reinterpret_cast<const T *>(pl->field[parity]);
     a.nxt = reinterpret_cast<T *>(pl->field[parity ^ 1]);
+    a.out = a.nxt;
     a.interior = pl->mask;
     a.sp = pl->sp;
     a.slots = reinterpret_cast<const T *>(pl->slots);
@@ -492,6 +503,128 @@ void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
     }
 }
 
+// Shapes of the two-step kernel: the largest p^(n+1) region (output rows +
+// 2) its shared memory holds and its ring depths.
+struct TbCfg {
+    int r2max, np, nq;
+};
+constexpr TbCfg TB_CFGS[] = {{24, 6, 4}, {16, 5, 2}};
+constexpr int TB_NCFG = 2;
+
+template <int R2MAX, int NP, int NQ>
+TmaKernel tb_kernel_of() {
+    return {(const void *)wk::interior_tb2<R2MAX, NP, NQ>, wk::tb_smem_of<R2MAX, NP, NQ>()};
+}
+TmaKernel tb_kernel(int cfg) { return cfg == 1 ? tb_kernel_of<16, 5, 2>() : tb_kernel_of<24, 6, 4>(); }
+
+// Buffers of a two-step pass with pair parity pp (steps t, t+1 of a chunk,
+// pp = t / 2 % 2): p^n, p^(n-1) in, p^(n+1), p^(n+2) out.  Pair parity 1
+// writes its levels back into field[1] and field[0], so every chunk, and the
+// single steps after the last full chunk, start from p^n in field[0].
+struct TbBufs {
+    float *cur, *old, *out1, *out2;
+};
+TbBufs tb_bufs(const wavey_cuda_plan *pl, int pp) {
+    auto f = [](void *p) { return static_cast<float *>(p); };
+    if (pp == 0) return {f(pl->field[0]), f(pl->field[1]), f(pl->field2[0]), f(pl->field2[1])};
+    return {f(pl->field2[1]), f(pl->field2[0]), f(pl->field[1]), f(pl->field[0])};
+}
+
+// Two steps (t, t+1) in one pass over the fields: step t's special cells and
+// receivers beside interior_tb2 (both levels of the interior), then
+// tb2_second (step t+1's shell and special cells, its receivers).
+void launch_pair_tb2(wavey_cuda_plan *pl, int t, int pp) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    cudaStream_t s = ctx->stream, side = ctx->side;
+    const TbBufs fb = tb_bufs(pl, pp);
+    wk::StepArgs<float> a;
+    fill_args<float>(pl, a, 0);
+    a.interior_blocks = 0;
+    a.cur = fb.cur;
+    a.nxt = fb.old;
+    a.out = fb.out1;
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = pl->branch % 3 == 1 ? pl->prio_hi : pl->prio_lo;
+    attr[1].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[1].val.accessPolicyWindow = pl->l2_window;
+    const int nattr = pl->l2_window.num_bytes ? 2 : 1;
+    const int branch_blocks = a.special_blocks + pl->record_blocks;
+    if (branch_blocks > 0) {
+        cudaEventRecord(pl->ev_fork, s);
+        cudaStreamWaitEvent(side, pl->ev_fork, 0);
+        cudaLaunchConfig_t lc = {};
+        lc.blockDim = dim3(wk::BLOCK);
+        lc.gridDim = dim3(branch_blocks);
+        lc.stream = side;
+        lc.attrs = attr;
+        lc.numAttrs = nattr;
+        switch (pl->branch / 3) {
+            case 1: cudaLaunchKernelEx(&lc, wk::special_branch<4, 3>, a, t); break;
+            case 2: cudaLaunchKernelEx(&lc, wk::special_branch<4, 4>, a, t); break;
+            default: cudaLaunchKernelEx(&lc, wk::special_branch<4, 1>, a, t); break;
+        }
+    }
+    if (pl->tb_blocks > 0) {
+        wk::Tb2Args ta;
+        ta.interior = pl->mask;
+        ta.deep = pl->deep;
+        ta.out1 = fb.out1;
+        ta.out2 = fb.out2;
+        ta.error = pl->err;
+        ta.cells_p = pl->cells_p;
+        ta.nxp = (int)pl->nxp;
+        ta.ny = (int)pl->ny;
+        ta.nz = (int)pl->nz;
+        ta.nxw = (int)(pl->nxp / 32);
+        ta.tiles_x = pl->tb_tiles_x;
+        ta.tiles_y = pl->tb_tiles_y;
+        ta.tiles_z = pl->tb_tiles_z;
+        ta.zt = pl->tb_zt;
+        ta.rows = pl->tb_rows;
+        ta.l2 = (float)(COURANT * COURANT);
+        const TmaKernel k = tb_kernel(pl->tb_cfg);
+        cudaLaunchConfig_t lc = {};
+        cudaLaunchAttribute pa[1];
+        pa[0].id = cudaLaunchAttributePriority;
+        pa[0].val.priority = pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo;
+        lc.gridDim = dim3(pl->tb_blocks);
+        lc.blockDim = dim3(256);
+        lc.dynamicSmemBytes = k.smem;
+        lc.stream = s;
+        lc.attrs = pa;
+        lc.numAttrs = 1;
+        void *args[] = {&pl->tb_p[pp], &pl->tb_q[pp], &ta};
+        cudaLaunchKernelExC(&lc, k.fn, args);
+    }
+    if (branch_blocks > 0) {
+        cudaEventRecord(pl->ev_join, side);
+        cudaStreamWaitEvent(s, pl->ev_join, 0);
+    }
+    wk::Tb2Second sb;
+    sb.a = a;
+    sb.a.cur = fb.out1;
+    sb.a.nxt = fb.cur;  // p^n is the older level of step t+1
+    sb.a.out = fb.out2;
+    sb.shell = pl->shell;
+    sb.n_shell = (int)pl->n_shell;
+    sb.shell_blocks = (int)((pl->n_shell * pl->chunks + wk::BLOCK - 1) / wk::BLOCK);
+    const int blocks = sb.shell_blocks + a.special_blocks + pl->record_blocks;
+    if (blocks > 0) {
+        cudaLaunchConfig_t lc = {};
+        lc.blockDim = dim3(wk::BLOCK);
+        lc.gridDim = dim3(blocks);
+        lc.stream = s;
+        lc.attrs = attr + 1;
+        lc.numAttrs = nattr - 1;
+        switch (pl->branch / 3) {
+            case 1: cudaLaunchKernelEx(&lc, wk::tb2_second<3>, sb, t + 1); break;
+            case 2: cudaLaunchKernelEx(&lc, wk::tb2_second<4>, sb, t + 1); break;
+            default: cudaLaunchKernelEx(&lc, wk::tb2_second<1>, sb, t + 1); break;
+        }
+    }
+}
+
 wk::HalfArgs half_args(const wavey_cuda_plan *pl, int parity) {
     wk::HalfArgs a;
     a.cur = reinterpret_cast<const __half *>(pl->field[parity]);
@@ -677,7 +810,10 @@ int build_graph(wavey_cuda_plan *pl) {
     int st = ctx->cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     if (st) return st;
     cudaEventRecordWithFlags(pl->ev_a, s, cudaEventRecordExternal);
-    for (int t = 0; t < wk::RING; t++) step(pl, t, t & 1);
+    if (pl->tb2)
+        for (int t = 0; t < wk::RING; t += 2) launch_pair_tb2(pl, t, (t >> 1) & 1);
+    else
+        for (int t = 0; t < wk::RING; t++) step(pl, t, t & 1);
     cudaEventRecordWithFlags(pl->ev_b, s, cudaEventRecordExternal);
     fold(pl, wk::RING);
     wk::advance_base<<<1, 1, 0, s>>>(pl->base, wk::RING);
@@ -843,6 +979,105 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
     const int64_t tb = (int64_t)pl->tma_tiles_x * pl->tma_tiles_y * pl->tma_tiles_z * pl->chunks;
     if (tb >= (1ll << 31)) return ctx->fail(WAVEY_E_LIMIT, "launch grid too large");
     pl->tma_blocks = (int)tb;
+    return WAVEY_OK;
+}
+
+// Shape of the two-step pass: kernel shape cfg (TB_CFGS), output rows per
+// tile and z-run.  Encodes its tensor maps (p^n with a two-cell ring, p^(n-1)
+// with a one-cell ring, per pair parity) and sizes the grid.
+int tb_shape(wavey_cuda_plan *pl, int cfg, int rows, int zt) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    EncodeTiled enc = encode_tiled();
+    if (!enc) return ctx->fail(WAVEY_E_CUDA, "the driver lacks cuTensorMapEncodeTiled");
+    rows = std::max(1, std::min(rows, TB_CFGS[cfg].r2max - 2));
+    zt = std::max(1, zt);
+    const int64_t nx = pl->nx, ny = pl->ny, nz = pl->nz;
+    const cuuint64_t dims[4] = {(cuuint64_t)(nx * 4), (cuuint64_t)ny, (cuuint64_t)nz, (cuuint64_t)pl->chunks};
+    const cuuint64_t strides[3] = {(cuuint64_t)(pl->nxp * 4 * 4), (cuuint64_t)(pl->nxp * ny * 4 * 4),
+                                   (cuuint64_t)(pl->cells_p * 4 * 4)};
+    const cuuint32_t box_p[4] = {(cuuint32_t)wk::TB_PROW, (cuuint32_t)(rows + 4), 1, 1};
+    const cuuint32_t box_q[4] = {(cuuint32_t)wk::TMA_ROW_FLOATS, (cuuint32_t)(rows + 2), 1, 1};
+    const cuuint32_t unit[4] = {1, 1, 1, 1};
+    for (int pp = 0; pp < 2; pp++) {
+        const TbBufs fb = tb_bufs(pl, pp);
+        CUresult r1 = enc(&pl->tb_p[pp], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, fb.cur, dims, strides, box_p, unit,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        CUresult r2 = enc(&pl->tb_q[pp], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, fb.old, dims, strides, box_q, unit,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r1 != CUDA_SUCCESS || r2 != CUDA_SUCCESS)
+            return ctx->fail(WAVEY_E_CUDA, "tensor map encoding failed (%d, %d)", (int)r1, (int)r2);
+    }
+    pl->tb_cfg = cfg;
+    pl->tb_rows = rows;
+    pl->tb_zt = zt;
+    pl->tb_tiles_x = (int)((nx - 2 + wk::TB_CELLS - 1) / wk::TB_CELLS);
+    pl->tb_tiles_y = (int)((ny - 2 + rows - 1) / rows);
+    pl->tb_tiles_z = (int)((nz - 2 + zt - 1) / zt);
+    const int64_t tb = (int64_t)pl->tb_tiles_x * pl->tb_tiles_y * pl->tb_tiles_z * pl->chunks;
+    if (tb >= (1ll << 31)) return ctx->fail(WAVEY_E_LIMIT, "launch grid too large");
+    pl->tb_blocks = (int)tb;
+    return WAVEY_OK;
+}
+
+// Two steps per pass: the deep-cell mask (interior cells whose six
+// neighbours are interior cells) and the shell list (the other interior
+// cells) from the interior mask, the two extra field buffers, and a shape:
+// the output rows that best fill whole waves of resident CTAs (one z-run per
+// column where a layer fills a wave), unless WAVEY_TB_CFG / WAVEY_TB_ROWS /
+// WAVEY_TB_ZT say otherwise.
+int tb_setup(wavey_cuda_plan *pl, const std::vector<uint32_t> &mask) {
+    wavey_cuda_ctx *ctx = pl->ctx;
+    const int64_t nx = pl->nx, ny = pl->ny, nz = pl->nz, nxw = pl->nxp / 32;
+    auto bit = [&](int64_t z, int64_t y, int64_t x) { return (mask[(size_t)((z * ny + y) * nxw + x / 32)] >> (x % 32)) & 1u; };
+    std::vector<uint32_t> deep(mask.size(), 0u), shell;
+    for (int64_t z = 1; z < nz - 1; z++)
+        for (int64_t y = 1; y < ny - 1; y++)
+            for (int64_t x = 1; x < nx - 1; x++) {
+                if (!bit(z, y, x)) continue;
+                if (bit(z, y, x - 1) && bit(z, y, x + 1) && bit(z, y - 1, x) && bit(z, y + 1, x) && bit(z - 1, y, x) &&
+                    bit(z + 1, y, x))
+                    deep[(size_t)((z * ny + y) * nxw + x / 32)] |= 1u << (x % 32);
+                else
+                    shell.push_back((uint32_t)((z * ny + y) * pl->nxp + x));
+            }
+    int st;
+    for (int k = 0; k < 2; k++)
+        if ((st = alloc(pl, &pl->field2[k], pl->field_bytes))) return st;
+    if ((st = upload(pl, &pl->deep, deep.data(), deep.size() * 4))) return st;
+    if ((st = upload(pl, &pl->shell, shell.data(), shell.size() * 4))) return st;
+    pl->n_shell = (int64_t)shell.size();
+    if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return st;
+    for (int cfg = 0; cfg < TB_NCFG; cfg++) {
+        const TmaKernel k = tb_kernel(cfg);
+        if ((st = ctx->cuda(cudaFuncSetAttribute(k.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)k.smem),
+                            "shared memory attribute")))
+            return st;
+    }
+    const int cfg = env_int("WAVEY_TB_CFG", 0, 0, TB_NCFG - 1);
+    int occ = 0;
+    const TmaKernel k = tb_kernel(cfg);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k.fn, 256, k.smem) != cudaSuccess) cudaGetLastError();
+    const int64_t slots = std::max<int64_t>(1, (int64_t)occ * ctx->sm_count);
+    const int64_t tiles_x = (nx - 2 + wk::TB_CELLS - 1) / wk::TB_CELLS;
+    int best_rows = TB_CFGS[cfg].r2max - 2, best_tz = 1;
+    double best = -1.0;
+    for (int rows = TB_CFGS[cfg].r2max - 2; rows >= 6; rows--) {
+        const int64_t layer = tiles_x * ((ny - 2 + rows - 1) / rows) * pl->chunks;
+        const int64_t tz = std::max<int64_t>(1, std::min<int64_t>(slots / layer, nz - 2));
+        const int64_t ctas = layer * tz, waves = (ctas + slots - 1) / slots;
+        const double score = (double)ctas / (double)(waves * slots) * rows / (rows + 2.0);
+        if (score > best + 1e-9) {
+            best = score;
+            best_rows = rows;
+            best_tz = (int)tz;
+        }
+    }
+    const int rows = env_int("WAVEY_TB_ROWS", best_rows, 1, TB_CFGS[cfg].r2max - 2);
+    const int zt = env_int("WAVEY_TB_ZT", (int)((nz - 2 + best_tz - 1) / best_tz), 1, 1 << 20);
+    if ((st = tb_shape(pl, cfg, rows, zt))) return st;
+    pl->tb2 = true;
     return WAVEY_OK;
 }
 
@@ -1210,6 +1445,8 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if ((st = tma_shape(pl, cfg, env_int("WAVEY_TMA_ZT", zt1, 1, 4096)))) return bail(st);
         pl->zalt = env_int("WAVEY_ZALT", 1, 0, 1) != 0;
         pl->tma = true;
+        if (precision == WAVEY_FP32 && pl->V == 4 && env_int("WAVEY_TBLOCK", 0, 0, 1))
+            if ((st = tb_setup(pl, mask))) return bail(st);
     }
     if ((st = ctx->cuda(cudaStreamSynchronize(ctx->stream), "upload sync"))) return bail(st);
     if (standalone && steps >= (size_t)wk::RING)
@@ -1227,6 +1464,8 @@ int plan_reset(wavey_cuda_plan *pl) {
     apply_l2(pl);
     for (int k = 0; k < 2; k++)
         if ((st = ctx->cuda(cudaMemsetAsync(pl->field[k], 0, pl->field_bytes, s), "memset"))) return st;
+    for (int k = 0; k < 2; k++)
+        if (pl->field2[k] && (st = ctx->cuda(cudaMemsetAsync(pl->field2[k], 0, pl->field_bytes, s), "memset"))) return st;
     if (pl->state_bytes) {
         if ((st = ctx->cuda(cudaMemsetAsync(pl->su, 0, pl->state_bytes, s), "memset"))) return st;
         if ((st = ctx->cuda(cudaMemsetAsync(pl->sg, 0, pl->state_bytes, s), "memset"))) return st;
@@ -2167,6 +2406,9 @@ int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
     info->tma_depth = pl->tma ? pl->tma_cfg : -1;
     info->branch = pl->tma ? pl->branch : -1;
     info->dft_fp64 = pl->precision == WAVEY_FP64 || pl->dft64 ? 1 : 0;
+    info->two_step = pl->tb2 ? 1 : 0;
+    info->two_step_rows = pl->tb2 ? pl->tb_rows : 0;
+    info->two_step_zt = pl->tb2 ? pl->tb_zt : 0;
     return WAVEY_OK;
 }
 
