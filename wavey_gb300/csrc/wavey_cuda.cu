@@ -23,7 +23,9 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <memory>
 #include <string>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -75,6 +77,15 @@ int env_int(const char *name, int dflt, int lo, int hi) {
     if (!v) return dflt;
     int x = atoi(v);
     return x < lo ? lo : (x > hi ? hi : x);
+}
+
+// Threads of the host-side loops (grid packing, conversions, reordering the
+// spectra): every hardware thread, or WAVEY_HOST_THREADS.  Set per loop, so
+// an OpenMP default inherited from the process (often 1) does not serialise
+// them.
+int host_threads() {
+    static const int n = env_int("WAVEY_HOST_THREADS", std::max(1, (int)std::thread::hardware_concurrency()), 1, 256);
+    return n;
 }
 
 }  // namespace
@@ -839,7 +850,8 @@ int build_graph(wavey_cuda_plan *pl) {
 template <class T>
 std::vector<T> convert(const double *src, size_t n) {
     std::vector<T> v(n);
-    for (size_t i = 0; i < n; i++) v[i] = (T)src[i];
+#pragma omp parallel for schedule(static) num_threads(host_threads()) if (n >= (1u << 16))
+    for (int64_t i = 0; i < (int64_t)n; i++) v[(size_t)i] = (T)src[i];
     return v;
 }
 
@@ -854,10 +866,11 @@ int upload_typed(wavey_cuda_plan *pl, void **out, const std::vector<double> &src
     return pl->ctx->cuda(cudaStreamSynchronize(pl->ctx->stream), "upload sync");
 }
 
-// Converts src to T into an existing device buffer and waits for the copy.
+// Converts n values at src to T into an existing device buffer and waits
+// for the copy.
 template <class T>
-int upload_into(wavey_cuda_plan *pl, void *dst, const std::vector<double> &src) {
-    std::vector<T> v = convert<T>(src.data(), src.size());
+int upload_into(wavey_cuda_plan *pl, void *dst, const double *src, size_t n) {
+    std::vector<T> v = convert<T>(src, n);
     pl->h2d_bytes += (int64_t)(v.size() * sizeof(T));
     if (v.empty()) return WAVEY_OK;
     int st = pl->ctx->cuda(cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, pl->ctx->stream),
@@ -1239,34 +1252,48 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     std::vector<std::vector<Special>> sp(nz);
     std::vector<int64_t> air_z(nz, 0), int_z(nz, 0);
     std::vector<int> bad_z(nz, 0);
-#pragma omp parallel for schedule(dynamic, 1)
+    // One plane per iteration; counts and mask words are built in locals and
+    // stored once (per plane, per 32 cells), so threads share no cache line
+    // cell by cell.
+#pragma omp parallel for schedule(dynamic, 1) num_threads(host_threads())
     for (int64_t z = 0; z < nz; z++) {
+        int64_t n_air = 0, n_int = 0;
+        int bad = 0;
         for (int64_t y = 0; y < ny; y++) {
-            for (int64_t x = 0; x < nx; x++) {
-                const int64_t i = (z * ny + y) * nx + x;
-                const uint8_t f = flags[i];
-                if (!(f & AIR)) continue;
-                if (x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1) {
-                    bad_z[z] = 1;
-                    continue;
+            const uint8_t *frow = flags + (z * ny + y) * nx;
+            const uint32_t *brow = bidx + (z * ny + y) * nx;
+            uint32_t *mrow = mask.data() + (size_t)((z * ny + y) * nxw);
+            for (int64_t x0 = 0; x0 < nx; x0 += 32) {
+                uint32_t word = 0;
+                const int64_t x1 = std::min<int64_t>(x0 + 32, nx);
+                for (int64_t x = x0; x < x1; x++) {
+                    const uint8_t f = frow[x];
+                    if (!(f & AIR)) continue;
+                    if (x == 0 || y == 0 || z == 0 || x == nx - 1 || y == ny - 1 || z == nz - 1) {
+                        bad = 1;
+                        continue;
+                    }
+                    const uint32_t b = brow[x];
+                    if (b != NO_BOUNDARY && (int64_t)b >= nb) {
+                        bad = 2;
+                        continue;
+                    }
+                    n_air++;
+                    if (f == (AIR | 63) && b == NO_BOUNDARY) {
+                        word |= 1u << (x - x0);
+                        n_int++;
+                    } else {
+                        const uint32_t ns = b == NO_BOUNDARY ? 0 : grid->bstart[b + 1] - grid->bstart[b];
+                        sp[z].push_back({(uint32_t)((z * ny + y) * pl->nxp + x), (uint32_t)(f & 63) | (ns << wk::META_SLOT_SHIFT),
+                                         b == NO_BOUNDARY ? 0u : grid->bstart[b]});
+                    }
                 }
-                const uint32_t b = bidx[i];
-                if (b != NO_BOUNDARY && (int64_t)b >= nb) {
-                    bad_z[z] = 2;
-                    continue;
-                }
-                air_z[z]++;
-                const int64_t ip = (z * ny + y) * pl->nxp + x;
-                if (f == (AIR | 63) && b == NO_BOUNDARY) {
-                    mask[(size_t)((z * ny + y) * nxw + x / 32)] |= 1u << (x % 32);
-                    int_z[z]++;
-                } else {
-                    const uint32_t ns = b == NO_BOUNDARY ? 0 : grid->bstart[b + 1] - grid->bstart[b];
-                    sp[z].push_back({(uint32_t)ip, (uint32_t)(f & 63) | (ns << wk::META_SLOT_SHIFT),
-                                     b == NO_BOUNDARY ? 0u : grid->bstart[b]});
-                }
+                mrow[x0 / 32] = word;
             }
         }
+        air_z[z] = n_air;
+        int_z[z] = n_int;
+        bad_z[z] = bad;
     }
     for (int64_t z = 0; z < nz; z++) {
         if (bad_z[z] == 1)
@@ -1352,8 +1379,6 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
                                         cudaMemcpyHostToDevice, ctx->stream), "upload")))
         return bail(st);
     pl->h2d_bytes += (int64_t)(pl->sp_host.size() * sizeof(uint4));
-    std::vector<double> slot_v(grid->slots ? grid->slots : (const double *)nullptr,
-                               grid->slots ? grid->slots + 4 * nslots : (const double *)nullptr);
     std::vector<double> sig_v;
     if (signal_stride == 0) {
         sig_v.assign(signals, signals + steps);
@@ -1371,11 +1396,11 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         recv_p[r] = (uint32_t)((z * ny + y) * pl->nxp + x);
     }
     if (precision == WAVEY_FP64) {
-        if ((st = upload_into<double>(pl, pl->slots, slot_v))) return bail(st);
+        if ((st = upload_into<double>(pl, pl->slots, grid->slots, grid->slots ? 4 * nslots : 0))) return bail(st);
         if ((st = upload_typed<double>(pl, &pl->tapw, tapw))) return bail(st);
         if ((st = upload_typed<double>(pl, &pl->sig, sig_v))) return bail(st);
     } else {
-        if ((st = upload_into<float>(pl, pl->slots, slot_v))) return bail(st);
+        if ((st = upload_into<float>(pl, pl->slots, grid->slots, grid->slots ? 4 * nslots : 0))) return bail(st);
         if ((st = upload_typed<float>(pl, &pl->tapw, tapw))) return bail(st);
         if ((st = upload_typed<float>(pl, &pl->sig, sig_v))) return bail(st);
     }
@@ -1984,19 +2009,24 @@ int plan_read(wavey_cuda_plan *pl, double *out, double *ir_out) {
     if (!pl->ran) return ctx->fail(WAVEY_E_INVALID, "the plan has not run");
     int st;
     if (out && pl->acc_bytes) {
+        // Copied into a zero-filled vector (its pages are in place before
+        // the copy), then reordered in one sequential pass over it: from
+        // [chunk][receiver][f][lane] to [source][receiver][f].  (Threads
+        // writing the caller's fresh pages contend on page faults.)
         std::vector<double> acc(pl->acc_bytes / sizeof(double));
         if ((st = ctx->cuda(cudaMemcpy(acc.data(), pl->acc, pl->acc_bytes, cudaMemcpyDeviceToHost), "read spectra"))) return st;
-        const int64_t R = pl->n_recv, F = pl->nf, V = pl->V;
-        for (int s = 0; s < pl->n_sources; s++) {
-            const int64_t c = s / V, l = s % V;
+        const int64_t R = pl->n_recv, F = pl->nf, V = pl->V, S = pl->n_sources;
+        const double *a = acc.data();
+        for (int64_t c = 0; c < pl->chunks; c++)
             for (int64_t r = 0; r < R; r++)
-                for (int64_t f = 0; f < F; f++) {
-                    const double *a = acc.data() + ((((c * R) + r) * F + f) * V + l) * 2;
-                    double *o = out + (((int64_t)s * R + r) * F + f) * 2;
-                    o[0] = a[0];
-                    o[1] = a[1];
-                }
-        }
+                for (int64_t f = 0; f < F; f++)
+                    for (int64_t l = 0; l < V; l++, a += 2) {
+                        const int64_t s = c * V + l;
+                        if (s >= S) continue;
+                        double *o = out + ((s * R + r) * F + f) * 2;
+                        o[0] = a[0];
+                        o[1] = a[1];
+                    }
     }
     if (ir_out) {
         if (!pl->want_ir) return ctx->fail(WAVEY_E_INVALID, "the plan records no time series");
@@ -2004,9 +2034,12 @@ int plan_read(wavey_cuda_plan *pl, double *out, double *ir_out) {
         if (pl->precision == WAVEY_FP64) {
             if ((st = ctx->cuda(cudaMemcpy(ir_out, pl->ir, pl->ir_bytes, cudaMemcpyDeviceToHost), "read ir"))) return st;
         } else {
-            std::vector<float> v(n);
-            if ((st = ctx->cuda(cudaMemcpy(v.data(), pl->ir, pl->ir_bytes, cudaMemcpyDeviceToHost), "read ir"))) return st;
-            for (size_t i = 0; i < n; i++) ir_out[i] = (double)v[i];
+            std::unique_ptr<float[]> v(new (std::nothrow) float[n]);
+            if (!v) return ctx->fail(WAVEY_E_NOMEM, "host allocation failed");
+            if ((st = ctx->cuda(cudaMemcpy(v.get(), pl->ir, pl->ir_bytes, cudaMemcpyDeviceToHost), "read ir"))) return st;
+            const float *src = v.get();
+#pragma omp parallel for schedule(static) num_threads(host_threads()) if (n >= (1u << 16))
+            for (int64_t i = 0; i < (int64_t)n; i++) ir_out[i] = (double)src[i];
         }
     }
     return WAVEY_OK;
