@@ -521,6 +521,73 @@ __global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const A *tw, d
     }
 }
 
+// The same fold for FP32 samples and sums, shaped as the small matrix
+// product it is: the chunk's twiddles are staged in shared memory once per
+// block ([t][f], frequencies padded to DFT_FB with zeros), and each thread
+// takes one (chunk, receiver) and DFT_FB frequencies, so every sample it
+// loads (coalesced across the receivers of a warp) feeds 2 x V x DFT_FB FMAs.
+// Each output still sums its steps in order with the same FMAs, so the
+// spectra are dft_chunk's bit for bit.  Used when the twiddles fit in
+// DFT_SMEM_MAX bytes.
+constexpr int DFT_FB = 4;
+constexpr int DFT_SMEM_MAX = 96 * 1024;
+__host__ __device__ constexpr int dft_nfp(int nf) { return (nf + DFT_FB - 1) / DFT_FB * DFT_FB; }
+
+template <int V>
+__global__ void __launch_bounds__(BLOCK) dft_chunk_tiled(const float *ring, const float *tw, double *acc, int n_recv,
+                                                         int nf, int chunks, int count, const long long *base,
+                                                         long long steps) {
+    extern __shared__ float2 s_tw[];
+    count = (int)min((long long)count, steps - *base);
+    const int nfp = dft_nfp(nf);
+    // Staged with one 8-byte load per twiddle, eight loads in flight per
+    // thread.
+    const float2 *tw2 = reinterpret_cast<const float2 *>(tw);
+#pragma unroll 8
+    for (int i = threadIdx.x; i < count * nfp; i += BLOCK) {
+        const int t = i / nfp, f = i - t * nfp;
+        s_tw[i] = f < nf ? __ldg(tw2 + t * nf + f) : make_float2(0.0f, 0.0f);
+    }
+    __syncthreads();
+    const int fblocks = nfp / DFT_FB;
+    const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    if (idx >= (long long)chunks * fblocks * n_recv) return;
+    const int r = (int)(idx % n_recv);
+    const long long rest = idx / n_recv;
+    const int fb = (int)(rest % fblocks), c = (int)(rest / fblocks);
+    float re[DFT_FB][V], im[DFT_FB][V];
+#pragma unroll
+    for (int k = 0; k < DFT_FB; k++)
+#pragma unroll
+        for (int l = 0; l < V; l++) re[k][l] = im[k][l] = 0.0f;
+    const float *src = ring + ((long long)c * RING * n_recv + r) * V;
+    const float2 *w = s_tw + fb * DFT_FB;
+#pragma unroll 8
+    for (int t = 0; t < count; t++) {
+        const Lanes<float, V> v = load<float, V, true>(src + (long long)t * n_recv * V);
+#pragma unroll
+        for (int k = 0; k < DFT_FB; k++) {
+            const float2 wk = w[t * nfp + k];
+#pragma unroll
+            for (int l = 0; l < V; l++) {
+                re[k][l] = fmaf(v.v[l], wk.x, re[k][l]);
+                im[k][l] = fmaf(v.v[l], wk.y, im[k][l]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < DFT_FB; k++) {
+        const int f = fb * DFT_FB + k;
+        if (f >= nf) break;
+        double *out = acc + (((long long)c * n_recv + r) * nf + f) * V * 2;
+#pragma unroll
+        for (int l = 0; l < V; l++) {
+            out[2 * l] += (double)re[k][l];
+            out[2 * l + 1] += (double)im[k][l];
+        }
+    }
+}
+
 // ir[s][r][n0 + t] = ring[c][t][r][l] (s = c*V + l): the time series of
 // run_cpu_ir (fdtd.rs:628-641).
 template <class T, int V>

@@ -2,9 +2,9 @@
 //
 // A CTA owns a tile of R rows x 128 floats of one z-run (32 cells of a
 // 4-source chunk, 64 cells of a 2-source chunk or 128 cells of one source)
-// and marches z, upwards on even steps and downwards on odd ones (TmaArgs::
-// rev), so that a step begins on the planes the previous step touched last:
-// on grids a few times the size of L2 those reads hit in L2.  One thread
+// and marches z -- FP32 fields upwards on even steps and downwards on odd
+// ones (TmaArgs::rev), so that a step begins on the planes the previous step
+// touched last: on grids a few times the size of L2 those reads hit in L2.  One thread
 // issues cp.async.bulk.tensor loads of whole planes several planes ahead
 // into a ring in shared memory:
 //
@@ -302,7 +302,10 @@ __host__ __device__ constexpr uint32_t tma_smem_of() {
 // special-cell kernel beside them) and LB = 3 (three CTAs per SM, more bytes
 // in flight where the interior dominates); the FP16 kernel, instruction-
 // bound, uses LB = 0, the compiler's own choice; SPEC caps at three CTAs.
-template <class E, int V, int R, int NP, int NQ, bool SPEC = false, int LB = 1>
+// ALT: the march direction follows TmaArgs::rev (FP32); FP16 kernels, whose
+// time is instruction issue rather than HBM, always march upwards and keep
+// the registers the choice would cost.
+template <class E, int V, int R, int NP, int NQ, bool SPEC = false, int LB = 1, bool ALT = (sizeof(E) == 4)>
 __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_constant__ CUtensorMap tm_p,
                                                     const __grid_constant__ CUtensorMap tm_q, TmaArgs<E> a,
                                                     const __grid_constant__ SpecTile sp) {
@@ -339,8 +342,9 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
     // the output planes as zs .. ze-1; downwards as ze, ze-1, .., zs-1 and
     // ze-1 .. zs.  Alternating it from step to step starts each step on the
     // planes the previous one touched last, which are still in L2.
-    const int dz = a.rev ? -1 : 1;
-    const int zq0 = a.rev ? ze - 1 : zs;   // first output plane
+    const bool rev = ALT && a.rev;
+    const int dz = rev ? -1 : 1;
+    const int zq0 = rev ? ze - 1 : zs;     // first output plane
     const int zp0 = zq0 - dz;              // first p plane
 
     // FP16: slab scales of the z-run -- p^n of planes zs-1..ze (2^E of level
@@ -447,8 +451,8 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
             const E *pc = Pbuf + bc * (PS / sizeof(E));
             const E *qo = Qbuf + bq * (QB / sizeof(E));
             // p^n of planes z - 1 and z + 1: behind and ahead in march order.
-            const E *pm = Pbuf + (a.rev ? bp : bm) * (PS / sizeof(E));
-            const E *pn = Pbuf + (a.rev ? bm : bp) * (PS / sizeof(E));
+            const E *pm = Pbuf + (rev ? bp : bm) * (PS / sizeof(E));
+            const E *pn = Pbuf + (rev ? bm : bp) * (PS / sizeof(E));
 #pragma unroll
             for (int r = 0; r < RT; r++) {
                 const uint32_t word = mw[r][0];

@@ -26,6 +26,7 @@
 #include <memory>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <unordered_map>
 #include <vector>
 
@@ -779,7 +780,18 @@ void launch_fold(wavey_cuda_plan *pl, int count) {
         wk::twiddle_chunk<A><<<(tw_threads + 255) / 256, 256, 0, s>>>(pl->freqs, (int)pl->nf, pl->dt, pl->base, count,
                                                                        (long long)pl->steps, reinterpret_cast<A *>(pl->tw));
     const long long total = (long long)pl->chunks * pl->n_recv * pl->nf;
-    if (total > 0)
+    const size_t tiled_smem = (size_t)wk::RING * wk::dft_nfp((int)pl->nf) * sizeof(float2);
+    bool tiled = false;
+    if constexpr (std::is_same<T, float>::value && std::is_same<A, float>::value) {
+        if (total > 0 && tiled_smem <= (size_t)wk::DFT_SMEM_MAX) {
+            const long long threads = (long long)pl->chunks * (wk::dft_nfp((int)pl->nf) / wk::DFT_FB) * pl->n_recv;
+            wk::dft_chunk_tiled<V><<<(unsigned)((threads + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, tiled_smem, s>>>(
+                reinterpret_cast<const float *>(pl->ring), reinterpret_cast<const float *>(pl->tw), pl->acc,
+                (int)pl->n_recv, (int)pl->nf, pl->chunks, count, pl->base, (long long)pl->steps);
+            tiled = true;
+        }
+    }
+    if (!tiled && total > 0)
         wk::dft_chunk<T, V, A><<<(unsigned)((total + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
             reinterpret_cast<const T *>(pl->ring), reinterpret_cast<const A *>(pl->tw), pl->acc, (int)pl->n_recv, (int)pl->nf,
             pl->chunks, count, pl->base, (long long)pl->steps);
@@ -2312,6 +2324,14 @@ int wavey_cuda_create(int device, wavey_cuda_ctx **out) {
         ctx->max_window = prop.accessPolicyMaxWindowSize;
         ctx->l2_bytes = (size_t)prop.l2CacheSize;
     }
+    // The tiled receiver fold stages up to DFT_SMEM_MAX bytes of twiddles.
+    for (const void *fn : {(const void *)wk::dft_chunk_tiled<1>, (const void *)wk::dft_chunk_tiled<2>,
+                           (const void *)wk::dft_chunk_tiled<4>})
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, wk::DFT_SMEM_MAX) != cudaSuccess) {
+            cudaGetLastError();
+            wavey_cuda_destroy(ctx);
+            return WAVEY_E_CUDA;
+        }
     *out = ctx;
     return WAVEY_OK;
 }
