@@ -105,6 +105,9 @@ typedef struct {
                                              created with WAVEY_TBLOCK=1): interior_tb2 beside the special-cell
                                              kernel, then the shell and special cells of the second step */
     int32_t two_step_rows, two_step_zt;   /* its output rows per tile and z-run */
+    int32_t programmatic;                 /* 1: each step's interior kernel is a programmatic dependent of the
+                                             previous step (FP32 plans where one interior wave and a special-cell
+                                             block fit on every SM together; WAVEY_PDL=0 turns it off) */
 } wavey_plan_info;
 
 int wavey_cuda_create(int device, wavey_cuda_ctx **out);

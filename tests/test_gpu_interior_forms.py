@@ -103,6 +103,34 @@ def test_march_direction_does_not_change_results(backend, library, precision, cf
 
 
 @pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_programmatic_launch_does_not_change_results(backend, library, lanes):
+    """Where one wave of interior CTAs and a special-cell block fit on every
+    SM, each step's interior kernel is a programmatic dependent of the
+    previous step (its CTAs may start early and wait in the kernel);
+    WAVEY_PDL=0 launches it after the previous step ends.  Same results."""
+    g, taps, sig, rcv, freqs = branch_room(library, 0.1)
+    comps = directional_components(g, (1.6, 1.3, 1.1))
+    sources = (comps + [taps])[:lanes]
+    sig = sig[:401]
+    out = []
+    for pdl in ("1", "0"):
+        os.environ.update(WAVEY_PDL=pdl, WAVEY_TMA_ZT="64")
+        try:
+            plan = backend.plan(g, sources, sig, rcv, freqs, ir=True)
+        finally:
+            for k in ("WAVEY_PDL", "WAVEY_TMA_ZT"):
+                del os.environ[k]
+        try:
+            assert plan.info()["programmatic"] == int(pdl)
+            plan.run()
+            out.append(plan.read())
+        finally:
+            plan.close()
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][0], out[1][0])
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
 @pytest.mark.parametrize("cfg", range(7))
 def test_special_cells_inside_the_march_agree(backend, library, lanes, cfg):
     """The fused form (WAVEY_BRANCH=9: every interior CTA also updates the

@@ -119,6 +119,7 @@ class WaveyPlanInfo(C.Structure):
         ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("graph_kernels", C.c_int64),
         ("interior_kernel", C.c_int32), ("tma_zt", C.c_int32), ("tma_depth", C.c_int32), ("branch", C.c_int32),
         ("dft_fp64", C.c_int32), ("two_step", C.c_int32), ("two_step_rows", C.c_int32), ("two_step_zt", C.c_int32),
+        ("programmatic", C.c_int32),
     ]
 
 

@@ -381,6 +381,11 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
     __syncthreads();
+    // Launched as a programmatic dependent of the previous step, the CTA
+    // may start before that step's kernels end: everything above reads
+    // only data that no step writes; from here on the fields are touched.
+    // (Without a programmatic dependency this returns at once.)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 
     int np_issued = 0, nq_issued = 0;  // thread 0 is the only issuer
     auto issue_p = [&]() {
@@ -434,6 +439,9 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
             if (np_issued < Kp) issue_p();
             if (nq_issued < Kq) issue_q();
         }
+        // On its last plane the CTA lets the next step's CTAs be scheduled
+        // (they wait above until this step has ended).
+        if (j == Kq - 1) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
         const int z = zq0 + dz * j;
         const int iz = z - zs;       // the plane within the z-run
         float scm = 1.0f, scc = 1.0f, scp = 1.0f, sco = 1.0f, sinv = 1.0f, slim = 0.0f;

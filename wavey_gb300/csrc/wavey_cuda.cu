@@ -95,6 +95,7 @@ struct wavey_cuda_ctx {
     int device = 0;
     int sm_count = 0;
     int max_persist_l2 = 0;     // bytes of L2 that may be set aside for persisting accesses
+    int64_t regs_per_sm = 0, smem_per_sm = 0, smem_reserved = 0, threads_per_sm = 0;
     int max_window = 0;         // largest access-policy window
     size_t l2_bytes = 0;        // L2 size
     size_t persist_set = 0;     // persisting set-aside now in force
@@ -165,6 +166,8 @@ struct wavey_cuda_plan {
     int tma_tiles_x = 0, tma_tiles_y = 0, tma_tiles_z = 0, tma_zt = 32, tma_blocks = 0;
     int tma_cfg = 0;      // shape of the TMA kernel, an index into TMA_CFGS
     bool zalt = true;     // alternate the interior's z-march direction from step to step
+    bool pdl = false;     // interior launched as a programmatic dependent of the previous step (FP32)
+    bool pdl_wanted = false;
     // Two steps per pass (FP32, four sources per chunk): two more field
     // buffers for p^(n+1) and p^(n+2), the deep-cell mask, the shell list and
     // the pass's tensor maps (per pair parity) and geometry.
@@ -404,20 +407,25 @@ TmaKernel tma_kernel(int cfg) {
     }
 }
 
+// pdl: launched as a programmatic dependent of the stream's previous work
+// (its CTAs may be scheduled while the previous step drains; the kernel
+// waits for it before touching the fields).
 template <class E, int V, bool SPEC>
 void launch_tma_cfg(int cfg, int blocks, cudaStream_t s, int prio, const CUtensorMap &p, const CUtensorMap &q,
-                    const wk::TmaArgs<E> &ta, const wk::SpecTile &sp) {
+                    const wk::TmaArgs<E> &ta, const wk::SpecTile &sp, bool pdl = false) {
     const TmaKernel k = tma_kernel<E, V, SPEC>(cfg);
     cudaLaunchConfig_t lc = {};
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributePriority;
     attr[0].val.priority = prio;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     lc.gridDim = dim3(blocks);
     lc.blockDim = dim3(256);
     lc.dynamicSmemBytes = k.smem;
     lc.stream = s;
     lc.attrs = attr;
-    lc.numAttrs = 1;
+    lc.numAttrs = pdl ? 2 : 1;
     void *args[] = {const_cast<CUtensorMap *>(&p), const_cast<CUtensorMap *>(&q), const_cast<wk::TmaArgs<E> *>(&ta),
                     const_cast<wk::SpecTile *>(&sp)};
     cudaLaunchKernelExC(&lc, k.fn, args);
@@ -508,7 +516,8 @@ void launch_step_tma(wavey_cuda_plan *pl, int t, int parity) {
                                        tma_args<float>(pl, t, parity), sp);
     else if (pl->tma_blocks > 0)
         launch_tma_cfg<float, V, false>(pl->tma_cfg, pl->tma_blocks, s, pl->branch % 3 == 2 ? pl->prio_hi : pl->prio_lo,
-                                        pl->tm_p[parity], pl->tm_q[parity], tma_args<float>(pl, t, parity), sp);
+                                        pl->tm_p[parity], pl->tm_q[parity], tma_args<float>(pl, t, parity), sp,
+                                        pl->pdl && t > 0);
     if (branch) {
         cudaEventRecord(pl->ev_join, side);
         cudaStreamWaitEvent(s, pl->ev_join, 0);
@@ -962,6 +971,8 @@ int tile_specials(wavey_cuda_plan *pl, int rows) {
     return st;
 }
 
+bool pdl_safe(const wavey_cuda_plan *pl);
+
 // Shape of the TMA interior kernel: tile rows and ring depths (TMA_CFGS[cfg])
 // and the z planes each CTA marches (zt).  Encodes the tensor maps, whose
 // boxes depend on the tile rows, and sizes the grid.
@@ -1004,6 +1015,7 @@ int tma_shape(wavey_cuda_plan *pl, int cfg, int zt) {
     const int64_t tb = (int64_t)pl->tma_tiles_x * pl->tma_tiles_y * pl->tma_tiles_z * pl->chunks;
     if (tb >= (1ll << 31)) return ctx->fail(WAVEY_E_LIMIT, "launch grid too large");
     pl->tma_blocks = (int)tb;
+    pl->pdl = pl->pdl_wanted && pdl_safe(pl);
     return WAVEY_OK;
 }
 
@@ -1104,6 +1116,39 @@ int tb_setup(wavey_cuda_plan *pl, const std::vector<uint32_t> &mask) {
     if ((st = tb_shape(pl, cfg, rows, zt))) return st;
     pl->tb2 = true;
     return WAVEY_OK;
+}
+
+// Whether the FP32 interior may be launched as a programmatic dependent of
+// the previous step: the special cells in their own kernel, the interior
+// grid within one wave, and room on every SM for one block of the
+// special-cell kernel beside the interior CTAs that fit there -- so that
+// next-step CTAs, waiting on an SM for this step to end, can never keep the
+// special-cell kernel they wait for from running.
+template <int V>
+bool pdl_safe_v(const wavey_cuda_plan *pl) {
+    const wavey_cuda_ctx *ctx = pl->ctx;
+    const TmaKernel k = tma_kernel<float, V, false>(pl->tma_cfg);
+    const void *sfn = pl->branch / 3 == 1 ? (const void *)wk::special_branch<V, 3>
+                      : pl->branch / 3 == 2 ? (const void *)wk::special_branch<V, 4>
+                                            : (const void *)wk::special_branch<V, 1>;
+    cudaFuncAttributes fi, fs;
+    int occ = 0;
+    if (cudaFuncGetAttributes(&fi, k.fn) != cudaSuccess || cudaFuncGetAttributes(&fs, sfn) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k.fn, 256, k.smem) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    auto regs = [](int per_thread, int threads) { return (int64_t)((per_thread + 7) / 8 * 8) * threads; };
+    const int64_t r = occ * regs(fi.numRegs, 256) + regs(fs.numRegs, wk::BLOCK);
+    const int64_t sm = occ * ((int64_t)k.smem + fi.sharedSizeBytes + ctx->smem_reserved) + fs.sharedSizeBytes + ctx->smem_reserved;
+    const int64_t th = occ * 256 + wk::BLOCK;
+    return occ > 0 && pl->tma_blocks <= (int64_t)occ * ctx->sm_count && r <= ctx->regs_per_sm && sm <= ctx->smem_per_sm &&
+           th <= ctx->threads_per_sm;
+}
+
+bool pdl_safe(const wavey_cuda_plan *pl) {
+    if (pl->precision != WAVEY_FP32 || pl->branch == BRANCH_FUSED || !pl->tma) return false;
+    return pl->V == 4 ? pdl_safe_v<4>(pl) : pl->V == 2 ? pdl_safe_v<2>(pl) : pdl_safe_v<1>(pl);
 }
 
 // Resident CTAs per SM of one shape of the TMA interior kernel.
@@ -1482,6 +1527,8 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         if ((st = tma_shape(pl, cfg, env_int("WAVEY_TMA_ZT", zt1, 1, 4096)))) return bail(st);
         pl->zalt = env_int("WAVEY_ZALT", 1, 0, 1) != 0;
         pl->tma = true;
+        pl->pdl_wanted = env_int("WAVEY_PDL", 1, 0, 1) != 0;
+        pl->pdl = pl->pdl_wanted && pdl_safe(pl);
         if (precision == WAVEY_FP32 && pl->V == 4 && env_int("WAVEY_TBLOCK", 0, 0, 1))
             if ((st = tb_setup(pl, mask))) return bail(st);
     }
@@ -2323,6 +2370,10 @@ int wavey_cuda_create(int device, wavey_cuda_ctx **out) {
         ctx->max_persist_l2 = prop.persistingL2CacheMaxSize;
         ctx->max_window = prop.accessPolicyMaxWindowSize;
         ctx->l2_bytes = (size_t)prop.l2CacheSize;
+        ctx->regs_per_sm = prop.regsPerMultiprocessor;
+        ctx->smem_per_sm = (int64_t)prop.sharedMemPerMultiprocessor;
+        ctx->smem_reserved = (int64_t)prop.reservedSharedMemPerBlock;
+        ctx->threads_per_sm = prop.maxThreadsPerMultiProcessor;
     }
     // The tiled receiver fold stages up to DFT_SMEM_MAX bytes of twiddles.
     for (const void *fn : {(const void *)wk::dft_chunk_tiled<1>, (const void *)wk::dft_chunk_tiled<2>,
@@ -2462,6 +2513,7 @@ int wavey_cuda_plan_info(const wavey_cuda_plan *pl, wavey_plan_info *info) {
     info->two_step = pl->tb2 ? 1 : 0;
     info->two_step_rows = pl->tb2 ? pl->tb_rows : 0;
     info->two_step_zt = pl->tb2 ? pl->tb_zt : 0;
+    info->programmatic = pl->pdl ? 1 : 0;
     return WAVEY_OK;
 }
 
