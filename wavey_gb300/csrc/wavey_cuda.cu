@@ -44,7 +44,7 @@ constexpr double COURANT = 0.5773502691896257;  // fdtd.rs:138
 constexpr uint64_t MAX_CELLS = 600000000ull;      // fdtd.rs:140
 constexpr uint32_t NO_BOUNDARY = 0xFFFFFFFFu;
 constexpr uint8_t AIR = 64;
-constexpr int ZT = 16;  // z planes marched by one interior CTA
+constexpr int ZT = 16;  // z planes marched by one interior CTA of the fused step kernel (default)
 
 // cuTensorMapEncodeTiled, fetched from the driver once (no link-time
 // dependency on libcuda).
@@ -157,6 +157,7 @@ struct wavey_cuda_plan {
     float *wmax = nullptr;         // FP16 storage: sum |tap weight| per source
     // launch geometry
     int tiles_x = 0, tiles_y = 0, tiles_z = 0;
+    int zt = ZT;  // z planes per interior CTA of the fused step kernel
     int interior_blocks = 0, special_blocks = 0, record_blocks = 0;
     cudaGraphExec_t graph = nullptr;
     int64_t graph_kernels = 0;  // kernel launches per replay of the chunk graph
@@ -329,7 +330,7 @@ void fill_args(wavey_cuda_plan *pl, wk::StepArgs<T> &a, int parity) {
     a.tiles_x = pl->tiles_x;
     a.tiles_y = pl->tiles_y;
     a.tiles_z = pl->tiles_z;
-    a.zt = ZT;
+    a.zt = pl->zt;
     a.interior_blocks = pl->interior_blocks;
     a.special_blocks = pl->special_blocks;
     a.record_blocks = pl->record_blocks;
@@ -678,7 +679,7 @@ wk::HalfArgs half_args(const wavey_cuda_plan *pl, int parity) {
     a.tiles_x = pl->tiles_x;
     a.tiles_y = pl->tiles_y;
     a.tiles_z = pl->tiles_z;
-    a.zt = ZT;
+    a.zt = pl->zt;
     a.interior_blocks = pl->interior_blocks;
     a.special_blocks = pl->special_blocks;
     a.record_blocks = pl->record_blocks;
@@ -1399,7 +1400,8 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     // Launch geometry.
     pl->tiles_x = (int)(pl->nxp / 32);
     pl->tiles_y = (int)((ny - 2 + wk::TILE_Y - 1) / wk::TILE_Y);
-    pl->tiles_z = (int)((nz - 2 + ZT - 1) / ZT);
+    pl->zt = env_int("WAVEY_FUSED_ZT", ZT, 1, 4096);
+    pl->tiles_z = (int)((nz - 2 + pl->zt - 1) / pl->zt);
     const int64_t ib = (int64_t)pl->tiles_x * pl->tiles_y * pl->tiles_z * pl->chunks;
     const int64_t sb = (pl->n_special * pl->chunks + wk::BLOCK - 1) / wk::BLOCK;
     const int64_t rb = (pl->n_recv * pl->chunks + wk::BLOCK - 1) / wk::BLOCK;
