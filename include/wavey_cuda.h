@@ -235,8 +235,10 @@ void wavey_cuda_grid_free(wavey_device_grid *grid);
  * own tile from the planes it stages, with only the receiver samples on the
  * concurrent kernel.  If form 9 wins, stage 3 times every interior shape
  * again with it.  Each candidate runs two 128-step chunks of the plan's own
- * grid, and the plan keeps the fastest.
- * result (nullable) lists the candidates' step times (every candidate: at
+ * grid (the second one timed); stage 4 times the four fastest again over up
+ * to four chunks each (plans of at least 640 steps), and the plan keeps the
+ * fastest of those.  result->step_us is the winner's last timing.
+ * result (nullable) lists the candidates' first step times (every candidate: at
  * most 14 shapes x 11 z-runs x 2 families, 9 other forms and the fused
  * form's 154 shapes, 471 in all).  Neither stage changes any arithmetic.
  * Other plans are left as they are. */

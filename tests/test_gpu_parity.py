@@ -87,7 +87,10 @@ def test_autotuned_plan_gives_identical_results(backend):
     before = plan.read()
     res = plan.autotune()
     assert res["candidates"] and res["step_us"] > 0
-    assert res["step_us"] == min(c[3] for c in res["candidates"])
+    # The winner is one of the candidates, and among the four fastest of the
+    # first timing (the confirmation stage re-times those four).
+    firsts = sorted(res["candidates"], key=lambda c: c[3])[:4]
+    assert (res["cfg"], res["zt"], res["branch"]) in [(c[0], c[1], c[2]) for c in firsts]
     plan.run()
     after = plan.read()
     assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])

@@ -131,6 +131,29 @@ __device__ __forceinline__ void ld4(const __half *p, float o[4], float sc) {
     o[3] = __high2float(b) * sc;
 }
 
+// Four consecutive FP16 elements of shared memory as stored (bit patterns).
+__device__ __forceinline__ void ld4h(const __half *p, uint16_t o[4]) {
+    const uint2 raw = *reinterpret_cast<const uint2 *>(p);
+    o[0] = (uint16_t)(raw.x & 0xffffu), o[1] = (uint16_t)(raw.x >> 16);
+    o[2] = (uint16_t)(raw.y & 0xffffu), o[3] = (uint16_t)(raw.y >> 16);
+}
+
+// c + h for an FP16 h, rounded once to nearest (sm_100's mixed-precision
+// add: h converts to FP32 exactly inside the add), so it equals
+// radd(c, float(h)) bit for bit with one instruction instead of two.
+__device__ __forceinline__ float radd_h(float c, uint16_t h) {
+    float r;
+    asm("add.rn.f32.f16 %0, %1, %2;" : "=f"(r) : "h"(h), "f"(c));
+    return r;
+}
+
+// a / b for slab scales a and b: powers of two in FP32's normal range, or
+// both zero (a level not yet written), whose ratio is taken as 1.  Exact, by
+// subtracting the exponents in the bit patterns.
+__device__ __forceinline__ float scale_ratio(float a, float b) {
+    return __int_as_float(__float_as_int(a) - __float_as_int(b) + 0x3f800000);
+}
+
 // The same without the slab scale: FP16 values as stored, converted exactly.
 __device__ __forceinline__ void ld4u(const float *p, float o[4]) { ld4(p, o, 1.0f); }
 __device__ __forceinline__ void ld4u(const __half *p, float o[4]) {
@@ -476,30 +499,60 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
                 // without the slab scale: it is a power of two, so the first
                 // three sums scaled once give the scaled sums bit for bit (FP16
                 // values scaled stay far inside FP32's normal range).
-                float w[12], vym[4], vyp[4], vod[4];
-                ld4u(rc + g - 4, w);
-                ld4u(rc + g + 4, w + 8);
-                ld4u(rc + g, w + 4);
-                float zmv[4], zpv[4];
-                ld4(pm + (row + 1) * PROW + g, zmv, scm);
-                ld4(pn + (row + 1) * PROW + g, zpv, scp);
-                ld4u(pc + row * PROW + g, vym);
-                ld4u(pc + (row + 2) * PROW + g, vyp);
+                float vod[4], nx4[4];
                 ld4(qo + row * TMA_ROW_FLOATS + lane * 4, vod, sco);
-                float nx4[4];
+                if constexpr (HALF) {
+                    // The x- neighbour and the centre are converted; the other
+                    // neighbours enter the sum through mixed-precision adds,
+                    // unscaled.  With A the plane's own four-neighbour sum,
+                    // the sum is ((A sc_z + zm sc_m) + zp sc_p), evaluated as
+                    // (((A sc_z/sc_m + zm) sc_m/sc_p + zp) sc_p: every scaling
+                    // is by a power of two in FP32's normal range, which
+                    // commutes with rounding, so each rounded sum is the
+                    // original one scaled, and the result is the same bits.
+                    float w[8];
+                    uint16_t hxp[12], hym[4], hyp[4], hzm[4], hzp[4];
+                    ld4u(rc + g - 4, w);
+                    ld4u(rc + g, w + 4);
+                    ld4h(rc + g - 4, hxp);
+                    ld4h(rc + g, hxp + 4);
+                    ld4h(rc + g + 4, hxp + 8);
+                    ld4h(pc + row * PROW + g, hym);
+                    ld4h(pc + (row + 2) * PROW + g, hyp);
+                    ld4h(pm + (row + 1) * PROW + g, hzm);
+                    ld4h(pn + (row + 1) * PROW + g, hzp);
+                    const float r_cm = scale_ratio(scc, scm), r_mp = scale_ratio(scm, scp);
 #pragma unroll
-                for (int e = 0; e < 4; e++) {
-                    float cv = w[4 + e];
-                    float s = radd(w[4 + e - V], w[4 + e + V]);
-                    s = radd(s, vym[e]);
-                    s = radd(s, vyp[e]);
-                    if constexpr (HALF) {
-                        cv = rmul(cv, scc);
-                        s = rmul(s, scc);
+                    for (int e = 0; e < 4; e++) {
+                        const float cv = rmul(w[4 + e], scc);
+                        float s = radd_h(w[4 + e - V], hxp[4 + e + V]);
+                        s = radd_h(s, hym[e]);
+                        s = radd_h(s, hyp[e]);
+                        s = radd_h(rmul(s, r_cm), hzm[e]);
+                        s = radd_h(rmul(s, r_mp), hzp[e]);
+                        s = rmul(s, scp);
+                        nx4[e] = radd(rsub(rmul(2.0f, cv), vod[e]), rmul(a.l2, rsub(s, rmul(6.0f, cv))));
                     }
-                    s = radd(s, zmv[e]);
-                    s = radd(s, zpv[e]);
-                    nx4[e] = radd(rsub(rmul(2.0f, cv), vod[e]), rmul(a.l2, rsub(s, rmul(6.0f, cv))));
+                } else {
+                    float zmv[4], zpv[4];
+                    ld4(pm + (row + 1) * PROW + g, zmv, scm);
+                    ld4(pn + (row + 1) * PROW + g, zpv, scp);
+                    float w[12], vym[4], vyp[4];
+                    ld4u(rc + g - 4, w);
+                    ld4u(rc + g + 4, w + 8);
+                    ld4u(rc + g, w + 4);
+                    ld4u(pc + row * PROW + g, vym);
+                    ld4u(pc + (row + 2) * PROW + g, vyp);
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const float cv = w[4 + e];
+                        float s = radd(w[4 + e - V], w[4 + e + V]);
+                        s = radd(s, vym[e]);
+                        s = radd(s, vyp[e]);
+                        s = radd(s, zmv[e]);
+                        s = radd(s, zpv[e]);
+                        nx4[e] = radd(rsub(rmul(2.0f, cv), vod[e]), rmul(a.l2, rsub(s, rmul(6.0f, cv))));
+                    }
                 }
                 E *dst = Q + (((long long)z * a.ny + (y0 + row)) * a.nxp + x0) * V;
                 if constexpr (HALF) {

@@ -2266,8 +2266,10 @@ int rooms_run(wavey_cuda_rooms *rm, const volatile int32_t *cancel, void (*progr
 // interior first at four blocks per SM, which fits beside a partial wave of
 // interior CTAs -- runs two 128-step chunks of this plan's own grid; the
 // fastest step span wins.  Stage 2: with that shape, every other form of the
-// special-cell update.  The plan keeps the winner.  Needs a TMA plan with at
-// least 256 steps.
+// special-cell update.  Stage 4: the four fastest distinct candidates again,
+// each over up to four timed chunks after a warm one, so that a one-chunk
+// timing's noise does not pick between near-equal candidates.  The plan keeps
+// the winner.  Needs a TMA plan with at least 256 steps.
 int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
     wavey_cuda_ctx *ctx = pl->ctx;
     if (res) *res = wavey_tune_result{};
@@ -2275,20 +2277,34 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
     int best_cfg = pl->tma_cfg, best_zt = pl->tma_zt, best_branch = pl->branch, n = 0, st;
     double best = 1e30;
     cudaStream_t s = ctx->stream;
-    auto trial = [&](int cfg, int zt, int branch) -> int {
+    struct Cand {
+        int cfg, zt, branch;
+        double us;
+    };
+    std::vector<Cand> all;
+    // Mean step span of chunks 2..reps+1 of the plan in shape (cfg, zt, branch).
+    auto timed = [&](int cfg, int zt, int branch, int reps, double *us) -> int {
         pl->branch = branch;
         if ((st = tma_shape(pl, cfg, zt))) return st;
         cudaGraphExecDestroy(pl->graph);
         pl->graph = nullptr;
         if ((st = build_graph(pl))) return st;
         if ((st = plan_reset(pl))) return st;
-        float ms = 0.f;
-        for (int rep = 0; rep < 2; rep++) {
+        double sum = 0.0;
+        for (int rep = 0; rep <= reps; rep++) {
+            float ms = 0.f;
             if ((st = ctx->cuda(cudaGraphLaunch(pl->graph, s), "graph launch"))) return st;
             if ((st = ctx->cuda(cudaEventSynchronize(pl->ev_b), "tune wait"))) return st;
-            cudaEventElapsedTime(&ms, pl->ev_a, pl->ev_b);  // the second chunk's span counts
+            cudaEventElapsedTime(&ms, pl->ev_a, pl->ev_b);
+            if (rep > 0) sum += ms;  // the first chunk warms up
         }
-        const double us = 1e3 * ms / wk::RING;
+        *us = 1e3 * sum / reps / wk::RING;
+        return WAVEY_OK;
+    };
+    auto trial = [&](int cfg, int zt, int branch) -> int {
+        double us = 0.0;
+        if ((st = timed(cfg, zt, branch, 1, &us))) return st;
+        all.push_back({cfg, zt, branch, us});
         if (res && n < WAVEY_TUNE_MAX) {
             res->cand_cfg[n] = cfg;
             res->cand_zt[n] = zt;
@@ -2323,6 +2339,24 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
         for (int cfg = 0; cfg < tma_ncfg(pl); cfg++)
             for (int zt : zts)
                 if (!(cfg == cfg1 && zt == zt1) && (st = trial(cfg, zt, BRANCH_FUSED))) return st;
+    }
+    // Stage 4: confirm among the fastest four (chunks the plan's own steps
+    // cover: its signals end there).
+    const int reps = (int)std::min<int64_t>(4, pl->steps / wk::RING - 1);
+    if (reps >= 2) {
+        std::sort(all.begin(), all.end(), [](const Cand &a, const Cand &b) { return a.us < b.us; });
+        double confirmed = 1e30;
+        for (size_t i = 0; i < all.size() && i < 4; i++) {
+            double us = 0.0;
+            if ((st = timed(all[i].cfg, all[i].zt, all[i].branch, reps, &us))) return st;
+            if (us < confirmed) {
+                confirmed = us;
+                best_cfg = all[i].cfg;
+                best_zt = all[i].zt;
+                best_branch = all[i].branch;
+            }
+        }
+        best = confirmed;
     }
     pl->branch = best_branch;
     if ((st = tma_shape(pl, best_cfg, best_zt))) return st;
