@@ -468,6 +468,12 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
         const int z = zq0 + dz * j;
         const int iz = z - zs;       // the plane within the z-run
         float scm = 1.0f, scc = 1.0f, scp = 1.0f, sco = 1.0f, sinv = 1.0f, slim = 0.0f;
+        // FP16: the update is evaluated in plane z's own scale (values
+        // divided by scc); the ratios between the planes' scales, all powers
+        // of two, carry the other terms into it.  A level not yet written has
+        // zero scales (all of level n at once, at n = 0; level n-1 at n <= 1)
+        // over zero fields.
+        float r_cm = 1.0f, r_mp = 1.0f, r_pk = 1.0f, r_ok = 1.0f, ksinv = 1.0f;
         if constexpr (HALF) {
             scm = ssc[iz];
             scc = ssc[iz + 1];
@@ -475,6 +481,11 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
             sco = ssc[TMA_SCALE_STRIDE + iz];
             sinv = ssc[2 * TMA_SCALE_STRIDE + iz];
             slim = ssc[3 * TMA_SCALE_STRIDE + iz];
+            r_cm = scale_ratio(scc, scm);
+            r_mp = scale_ratio(scm, scp);
+            r_pk = scale_ratio(scp, scc);
+            r_ok = sco == 0.0f ? 0.0f : scale_ratio(sco, scc);
+            ksinv = scc * sinv;
         }
         ok = ok && mbar_wait(barP + 8 * bp, php) && mbar_wait(barQ + 8 * bq, phq);
         uint32_t mb = 0;  // FP16: largest |p^(n+1)| stored, as float bits
@@ -500,16 +511,20 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
                 // three sums scaled once give the scaled sums bit for bit (FP16
                 // values scaled stay far inside FP32's normal range).
                 float vod[4], nx4[4];
-                ld4(qo + row * TMA_ROW_FLOATS + lane * 4, vod, sco);
+                ld4(qo + row * TMA_ROW_FLOATS + lane * 4, vod, HALF ? r_ok : sco);
                 if constexpr (HALF) {
                     // The x- neighbour and the centre are converted; the other
                     // neighbours enter the sum through mixed-precision adds,
                     // unscaled.  With A the plane's own four-neighbour sum,
-                    // the sum is ((A sc_z + zm sc_m) + zp sc_p), evaluated as
-                    // (((A sc_z/sc_m + zm) sc_m/sc_p + zp) sc_p: every scaling
-                    // is by a power of two in FP32's normal range, which
-                    // commutes with rounding, so each rounded sum is the
-                    // original one scaled, and the result is the same bits.
+                    // the sum is ((A sc_z + zm sc_m) + zp sc_p), evaluated in
+                    // plane z's scale as ((A sc_z/sc_m + zm) sc_m/sc_p + zp)
+                    // sc_p/sc_z, and the whole update with it (p^(n-1) as
+                    // q sc_o/sc_z; the store multiplies by sc_z 2^-E of level
+                    // n+1).  Every scaling is by a power of two in FP32's
+                    // normal range, which commutes with rounding (FP16 values
+                    // times scales of 2^-60 and more stay far above FP32's
+                    // subnormals), so each rounded value is the original one
+                    // scaled, and the stored result has the same bits.
                     float w[8];
                     uint16_t hxp[12], hym[4], hyp[4], hzm[4], hzp[4];
                     ld4u(rc + g - 4, w);
@@ -524,13 +539,13 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
                     const float r_cm = scale_ratio(scc, scm), r_mp = scale_ratio(scm, scp);
 #pragma unroll
                     for (int e = 0; e < 4; e++) {
-                        const float cv = rmul(w[4 + e], scc);
+                        const float cv = w[4 + e];
                         float s = radd_h(w[4 + e - V], hxp[4 + e + V]);
                         s = radd_h(s, hym[e]);
                         s = radd_h(s, hyp[e]);
                         s = radd_h(rmul(s, r_cm), hzm[e]);
                         s = radd_h(rmul(s, r_mp), hzp[e]);
-                        s = rmul(s, scp);
+                        s = rmul(s, r_pk);
                         nx4[e] = radd(rsub(rmul(2.0f, cv), vod[e]), rmul(a.l2, rsub(s, rmul(6.0f, cv))));
                     }
                 } else {
@@ -556,8 +571,8 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
                 }
                 E *dst = Q + (((long long)z * a.ny + (y0 + row)) * a.nxp + x0) * V;
                 if constexpr (HALF) {
-                    const __half2 h01 = __floats2half2_rn(nx4[0] * sinv, nx4[1] * sinv);
-                    const __half2 h23 = __floats2half2_rn(nx4[2] * sinv, nx4[3] * sinv);
+                    const __half2 h01 = __floats2half2_rn(nx4[0] * ksinv, nx4[1] * ksinv);
+                    const __half2 h23 = __floats2half2_rn(nx4[2] * ksinv, nx4[3] * ksinv);
 #pragma unroll
                     for (int e = 0; e < 4; e++)
                         if ((bits >> (e / V)) & 1u) mb = max(mb, __float_as_uint(nx4[e]) & 0x7fffffffu);
@@ -604,6 +619,9 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
             }
         }
         if constexpr (HALF) {
+            // The row maxima were taken in plane z's scale: back to the
+            // field's own (exact; NaN stays NaN).
+            mb = __float_as_uint(__uint_as_float(mb) * scc);
             // A value beyond the FP16 range of its slab scale is an error,
             // not a saturation.
             if (mb > __float_as_uint(slim) && *reinterpret_cast<volatile int *>(a.error) == 0)
