@@ -234,8 +234,9 @@ void wavey_cuda_grid_free(wavey_device_grid *grid);
  * form 9 (FP32 plans) has every interior CTA update the special cells of its
  * own tile from the planes it stages, with only the receiver samples on the
  * concurrent kernel.  If form 9 wins, stage 3 times every interior shape
- * again with it.  Each candidate runs two 128-step chunks of the plan's own
- * grid (the second one timed); stage 4 times the four fastest again over up
+ * again with it.  Each candidate runs three 128-step chunks of the plan's own
+ * grid (the last two timed; two chunks, one timed, for plans of under 384
+ * steps); stage 4 times the four fastest again over up
  * to four chunks each (plans of at least 640 steps), and the plan keeps the
  * fastest of those.  result->step_us is the winner's last timing.
  * result (nullable) lists the candidates' first step times (every candidate: at

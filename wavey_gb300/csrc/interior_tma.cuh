@@ -154,6 +154,14 @@ __device__ __forceinline__ float scale_ratio(float a, float b) {
     return __int_as_float(__float_as_int(a) - __float_as_int(b) + 0x3f800000);
 }
 
+// max(m, |x|) with NaN propagated (a NaN among the maxima must reach the
+// range check).
+__device__ __forceinline__ float max_abs_nan(float m, float x) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(m), "f"(fabsf(x)));
+    return r;
+}
+
 // The same without the slab scale: FP16 values as stored, converted exactly.
 __device__ __forceinline__ void ld4u(const float *p, float o[4]) { ld4(p, o, 1.0f); }
 __device__ __forceinline__ void ld4u(const __half *p, float o[4]) {
@@ -489,6 +497,7 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
         }
         ok = ok && mbar_wait(barP + 8 * bp, php) && mbar_wait(barQ + 8 * bq, phq);
         uint32_t mb = 0;  // FP16: largest |p^(n+1)| stored, as float bits
+        float mbf = 0.0f; // FP16: the same while the rows run, in plane z's scale
         if (ok) {
             const E *pc = Pbuf + bc * (PS / sizeof(E));
             const E *qo = Qbuf + bq * (QB / sizeof(E));
@@ -575,7 +584,7 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
                     const __half2 h23 = __floats2half2_rn(nx4[2] * ksinv, nx4[3] * ksinv);
 #pragma unroll
                     for (int e = 0; e < 4; e++)
-                        if ((bits >> (e / V)) & 1u) mb = max(mb, __float_as_uint(nx4[e]) & 0x7fffffffu);
+                        if ((bits >> (e / V)) & 1u) mbf = max_abs_nan(mbf, nx4[e]);
                     if (bits == GROUP) {
                         uint2 raw;
                         raw.x = *reinterpret_cast<const unsigned int *>(&h01);
@@ -620,8 +629,9 @@ __global__ void __launch_bounds__(256, SPEC ? 3 : LB) interior_tma(const __grid_
         }
         if constexpr (HALF) {
             // The row maxima were taken in plane z's scale: back to the
-            // field's own (exact; NaN stays NaN).
-            mb = __float_as_uint(__uint_as_float(mb) * scc);
+            // field's own (exact; NaN stays NaN, and its bits exceed any
+            // finite limit's).
+            mb = __float_as_uint(mbf * scc);
             // A value beyond the FP16 range of its slab scale is an error,
             // not a saturation.
             if (mb > __float_as_uint(slim) && *reinterpret_cast<volatile int *>(a.error) == 0)

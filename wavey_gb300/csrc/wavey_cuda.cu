@@ -1501,7 +1501,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
         // resident CTAs, and beside it the special-cell kernel -- FP32: capped
         // at four blocks per SM with the interior first, so that one of its
         // blocks fits on every SM beside two interior CTAs; FP16: three blocks
-        // per SM, equal priority -- the forms the autotuner picks on the
+        // per SM with the interior first -- the forms measured fastest on the
         // pillar room.
         cudaError_t e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 1>() : tma_attrs<float, 1>();
         if (e == cudaSuccess) e = precision == WAVEY_FP16_STORAGE ? tma_attrs<__half, 2>() : tma_attrs<float, 2>();
@@ -1520,7 +1520,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
             const int64_t layer = ((nx + cells_row - 1) / cells_row) * ((ny - 2 + 15) / 16) * pl->chunks;
             many_waves = layer >= 2 * 2 * (int64_t)ctx->sm_count;
         }
-        pl->branch = env_int("WAVEY_BRANCH", precision == WAVEY_FP32 ? (many_waves ? 3 : 8) : 3, 0,
+        pl->branch = env_int("WAVEY_BRANCH", precision == WAVEY_FP32 ? (many_waves ? 3 : 8) : 5, 0,
                              precision == WAVEY_FP32 ? BRANCH_FUSED : BRANCH_FUSED - 1);
         const int cfg = env_int("WAVEY_TMA_CFG", precision == WAVEY_FP16_STORAGE ? 6 : (many_waves ? 11 : 4), 0,
                                 tma_ncfg(pl) - 1);
@@ -2303,7 +2303,7 @@ int plan_autotune(wavey_cuda_plan *pl, wavey_tune_result *res) {
     };
     auto trial = [&](int cfg, int zt, int branch) -> int {
         double us = 0.0;
-        if ((st = timed(cfg, zt, branch, 1, &us))) return st;
+        if ((st = timed(cfg, zt, branch, pl->steps >= 3 * wk::RING ? 2 : 1, &us))) return st;
         all.push_back({cfg, zt, branch, us});
         if (res && n < WAVEY_TUNE_MAX) {
             res->cand_cfg[n] = cfg;
