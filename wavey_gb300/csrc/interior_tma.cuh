@@ -26,11 +26,12 @@
 //
 // The same kernel serves FP16 storage (E = __half): the rings then hold FP16
 // planes (a row is still 128 elements, the x halo 8 elements = 16 bytes so
-// every box starts on a 16-byte boundary), values are scaled by their slab's
-// power of two as they leave shared memory, p^(n+1) is stored with the next
-// level's scale, and every warp raises its slab maximum -- the operations of
-// fdtd_step_half's interior role in the same order, so the two give identical
-// results.
+// every box starts on a 16-byte boundary), p^(n+1) is stored with the next
+// level's scale, and every warp raises its slab maximum.  The update is that
+// of fdtd_step_half's interior role (every value scaled by its slab's power
+// of two, the same FP32 operations in the same order), evaluated in the
+// centre plane's own scale with most neighbours entering through
+// mixed-precision adds (see the row loop): the two give identical results.
 //
 // With SPEC (FP32 only) the CTA also updates the special cells of its tile:
 // after the interior cells of plane z it takes the tile's special cells of
