@@ -102,6 +102,27 @@ def test_march_direction_does_not_change_results(backend, library, precision, cf
         assert np.array_equal(out[0][0], out[1][0]), zt
 
 
+@pytest.mark.parametrize("precision", [FP32, FP16_STORAGE], ids=["fp32", "fp16"])
+def test_fused_kernel_z_run_does_not_change_results(backend, library, precision):
+    """The fused step kernel (WAVEY_INTERIOR=regq; FP64 plans and multi-room
+    runs use it too) splits z into runs of WAVEY_FUSED_ZT planes per CTA:
+    runs of 1, 5 and 64 planes give the default's (16) results bit for bit."""
+    g, taps, sig, rcv, freqs = branch_room(library, 0.1)
+    sources = directional_components(g, (1.6, 1.3, 1.1)) + [taps]
+    sig = sig[:300]
+    out = []
+    for zt in ("16", "1", "5", "64"):
+        os.environ.update(WAVEY_INTERIOR="regq", WAVEY_FUSED_ZT=zt)
+        try:
+            out.append(backend.run_batch(g, sources, sig, rcv, freqs, precision=precision, ir=True))
+        finally:
+            for k in ("WAVEY_INTERIOR", "WAVEY_FUSED_ZT"):
+                del os.environ[k]
+    for got in out[1:]:
+        assert np.array_equal(got[1], out[0][1])
+        assert np.array_equal(got[0], out[0][0])
+
+
 @pytest.mark.parametrize("lanes", [1, 2, 4])
 def test_programmatic_launch_does_not_change_results(backend, library, lanes):
     """Where one wave of interior CTAs and a special-cell block fit on every
