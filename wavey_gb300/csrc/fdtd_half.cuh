@@ -45,7 +45,8 @@ struct HalfArgs {
     const float *sig;          // [lanes_total][sig_stride]
     const float *wmax;         // [lanes_total] sum of |tap weight| per source
     const uint32_t *recv;
-    float *ring;               // [chunks][RING][n_recv][V]
+    float *ring;               // [chunks][RING][n_recv][V], or two rings ring_stride apart (StepArgs::ring)
+    long long ring_stride;
     const long long *base;
     unsigned int *amax;        // [AMAX_RING][chunks][nz] slab maxima as float bits
     float2 *scale;             // [SCALE_RING][chunks][nz] (2^E, 2^-E) of a time level
@@ -239,7 +240,8 @@ __device__ __forceinline__ void record_half(const HalfArgs &a, long long k, int 
     const long long cell = a.recv[r];
     const __half *P = a.cur + (long long)c * a.cells_p * V;
     const Lanes<float, V> v = load_h<V>(P + cell * V, slab_scale(a, n, c, (int)(cell / ((long long)a.nxp * a.ny))).x);
-    store<float, V>(a.ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
+    float *ring = a.ring + ((*a.base / RING) & 1) * a.ring_stride;
+    store<float, V>(ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
 }
 
 template <int V>

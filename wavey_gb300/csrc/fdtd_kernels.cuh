@@ -19,7 +19,9 @@
 //             (the samples of fdtd.rs:674-683, taken before the update).
 //
 // Every 128 steps a twiddle kernel and a DFT kernel fold the ring into the
-// FP64 receiver spectra; see dft_chunk below.
+// FP64 receiver spectra; see dft_chunk below.  Standalone plans keep two
+// rings, used by alternate chunks, and fold each chunk while the next one
+// runs.
 //
 // Fields are source-interleaved: a chunk of V right-hand sides (V = 1, 2 or
 // 4) stores the V values of a cell contiguously, so one 128-bit access
@@ -122,7 +124,9 @@ struct StepArgs {
     const T *tapw;             // [n_tap_rows][lanes_total] merged tap weight per source
     const T *sig;              // [lanes_total][sig_stride] or one shared row (sig_stride 0)
     const uint32_t *recv;      // [n_recv] padded receiver cells
-    T *ring;                   // [chunks][RING][n_recv][V]
+    T *ring;                   // [chunks][RING][n_recv][V], or two such rings (ring_stride apart) used by
+                               // alternate chunks, so that one is folded while the next chunk fills the other
+    long long ring_stride;     // elements between the two rings; 0: one ring
     const long long *base;     // step index of the chunk's first step
     long long cells_p;         // padded cells per chunk
     long long sig_stride;
@@ -339,7 +343,8 @@ __device__ __forceinline__ void record_one(const StepArgs<T> &a, long long k, in
     const long long r = k - (long long)c * a.n_recv;
     const T *P = a.cur + (long long)c * a.cells_p * V;
     const Lanes<T, V> v = load<T, V, true>(P + (long long)a.recv[r] * V);
-    store<T, V>(a.ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
+    T *ring = a.ring + ((*a.base / RING) & 1) * a.ring_stride;
+    store<T, V>(ring + (((long long)c * RING + t) * a.n_recv + r) * V, v);
 }
 
 // ------------------------------------------------------------------ step
@@ -471,14 +476,18 @@ __global__ void __launch_bounds__(BLOCK) fdtd_step_rooms(const RoomStep<T> *room
 // ------------------------------------------------------------- twiddles
 // tw[t][f] = exp(-j 2 pi frac(f dt n)) for n = base + t, phase in FP64
 // exactly as fdtd.rs:680 forms it.
+// The chunk folded starts at step *base - lag: lag = RING folds the previous
+// chunk (beside the steps of the current one); nothing before step 0.
 template <class T>
 __global__ void twiddle_chunk(const double *freqs, int nf, double dt, const long long *base, int count, long long steps,
-                              T *tw) {
-    count = (int)min((long long)count, steps - *base);  // a room that stops inside the chunk
+                              T *tw, int lag) {
+    const long long b0 = *base - lag;
+    if (b0 < 0) return;
+    count = (int)min((long long)count, steps - b0);  // a room that stops inside the chunk
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= count * nf) return;
     const int t = idx / nf, f = idx - t * nf;
-    const double x = freqs[f] * dt * (double)(*base + t);
+    const double x = freqs[f] * dt * (double)(b0 + t);
     const double ph = -6.283185307179586 * (x - trunc(x));
     double s, c;
     sincos(ph, &s, &c);
@@ -492,8 +501,12 @@ __global__ void twiddle_chunk(const double *freqs, int nf, double dt, const long
 // samples), added into FP64.  One thread per (chunk, receiver, freq).
 template <class T, int V, class A = T>
 __global__ void __launch_bounds__(BLOCK) dft_chunk(const T *ring, const A *tw, double *acc, int n_recv, int nf, int chunks,
-                                                   int count, const long long *base, long long steps) {
-    count = (int)min((long long)count, steps - *base);
+                                                   int count, const long long *base, long long steps, int lag,
+                                                   long long ring_stride) {
+    const long long b0 = *base - lag;
+    if (b0 < 0) return;
+    count = (int)min((long long)count, steps - b0);
+    ring += ((b0 / RING) & 1) * ring_stride;
     const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
     const long long total = (long long)chunks * n_recv * nf;
     if (idx >= total) return;
@@ -536,9 +549,12 @@ __host__ __device__ constexpr int dft_nfp(int nf) { return (nf + DFT_FB - 1) / D
 template <int V>
 __global__ void __launch_bounds__(BLOCK) dft_chunk_tiled(const float *ring, const float *tw, double *acc, int n_recv,
                                                          int nf, int chunks, int count, const long long *base,
-                                                         long long steps) {
+                                                         long long steps, int lag, long long ring_stride) {
     extern __shared__ float2 s_tw[];
-    count = (int)min((long long)count, steps - *base);
+    const long long b0 = *base - lag;
+    if (b0 < 0) return;  // the same for every thread: no barrier is left waiting
+    count = (int)min((long long)count, steps - b0);
+    ring += ((b0 / RING) & 1) * ring_stride;
     const int nfp = dft_nfp(nf);
     // Staged with one 8-byte load per twiddle, eight loads in flight per
     // thread.
@@ -592,9 +608,12 @@ __global__ void __launch_bounds__(BLOCK) dft_chunk_tiled(const float *ring, cons
 // run_cpu_ir (fdtd.rs:628-641).
 template <class T, int V>
 __global__ void ir_chunk(const T *ring, T *ir, int n_recv, int chunks, int n_sources, long long steps,
-                         const long long *base, int count) {
+                         const long long *base, int count, int lag, long long ring_stride) {
     const int full = count;
-    count = (int)min((long long)count, steps - *base);
+    const long long b0 = *base - lag;
+    if (b0 < 0) return;
+    count = (int)min((long long)count, steps - b0);
+    ring += ((b0 / RING) & 1) * ring_stride;
     const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
     const long long total = (long long)chunks * V * n_recv * full;
     if (idx >= total) return;
@@ -606,7 +625,7 @@ __global__ void ir_chunk(const T *ring, T *ir, int n_recv, int chunks, int n_sou
     const int s = (int)rest;  // c * V + l
     if (s >= n_sources) return;
     const int c = s / V, l = s - c * V;
-    ir[((long long)s * n_recv + r) * steps + *base + t] = ring[(((long long)c * RING + t) * n_recv + r) * V + l];
+    ir[((long long)s * n_recv + r) * steps + b0 + t] = ring[(((long long)c * RING + t) * n_recv + r) * V + l];
 }
 
 // Per-speaker transfer functions from a plan's spectra accumulators, as

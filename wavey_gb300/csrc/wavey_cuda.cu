@@ -102,6 +102,7 @@ struct wavey_cuda_ctx {
     const void *persist_owner = nullptr;  // the plan whose set-aside and lines are in force
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;  // the special-cell branch of a TMA step
+    cudaStream_t folds = nullptr; // the previous chunk's receiver fold, beside a chunk's steps
     std::mutex mu;
     std::string err;
     char name[256] = {0};
@@ -167,6 +168,11 @@ struct wavey_cuda_plan {
     int tma_tiles_x = 0, tma_tiles_y = 0, tma_tiles_z = 0, tma_zt = 32, tma_blocks = 0;
     int tma_cfg = 0;      // shape of the TMA kernel, an index into TMA_CFGS
     bool zalt = true;     // alternate the interior's z-march direction from step to step
+    // Two receiver rings used by alternate chunks: each chunk's graph folds
+    // the previous chunk's ring on the fold stream beside its own steps.
+    bool fold_overlap = false;
+    int64_t ring_stride = 0;  // elements between the two rings
+    cudaEvent_t ev_ffork = nullptr, ev_fjoin = nullptr;
     bool pdl = false;     // interior launched as a programmatic dependent of the previous step (FP32)
     bool pdl_wanted = false;
     // Two steps per pass (FP32, four sources per chunk): two more field
@@ -208,7 +214,8 @@ struct wavey_cuda_plan {
             cudaCtxResetPersistingL2Cache();
             ctx->persist_owner = nullptr;
         }
-        for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1, inflight[0], inflight[1], inflight[2], inflight[3], ev_fork, ev_join})
+        for (cudaEvent_t e : {ev_a, ev_b, ev_t0, ev_t1, inflight[0], inflight[1], inflight[2], inflight[3], ev_fork, ev_join,
+                              ev_ffork, ev_fjoin})
             if (e) cudaEventDestroy(e);
         for (DevBuf &b : bufs)
             if (b.p) cudaFree(b.p);
@@ -315,6 +322,7 @@ void fill_args(wavey_cuda_plan *pl, wk::StepArgs<T> &a, int parity) {
     a.sig = reinterpret_cast<const T *>(pl->sig);
     a.recv = pl->recv;
     a.ring = reinterpret_cast<T *>(pl->ring);
+    a.ring_stride = pl->ring_stride;
     a.base = pl->base;
     a.cells_p = pl->cells_p;
     a.sig_stride = pl->sig_stride;
@@ -661,6 +669,7 @@ wk::HalfArgs half_args(const wavey_cuda_plan *pl, int parity) {
     a.wmax = pl->wmax;
     a.recv = pl->recv;
     a.ring = reinterpret_cast<float *>(pl->ring);
+    a.ring_stride = pl->ring_stride;
     a.base = pl->base;
     a.amax = pl->amax;
     a.scale = pl->scale;
@@ -783,12 +792,11 @@ void step(wavey_cuda_plan *pl, int t, int parity) {
 // A: the type of the twiddles and of the chunk sums (T, or FP64 for FP32
 // samples in a plan with FP64 receiver accumulation).
 template <class T, int V, class A = T>
-void launch_fold(wavey_cuda_plan *pl, int count) {
-    cudaStream_t s = pl->ctx->stream;
+void launch_fold(wavey_cuda_plan *pl, int count, int lag, cudaStream_t s) {
     const int tw_threads = count * (int)pl->nf;
     if (tw_threads > 0)
         wk::twiddle_chunk<A><<<(tw_threads + 255) / 256, 256, 0, s>>>(pl->freqs, (int)pl->nf, pl->dt, pl->base, count,
-                                                                       (long long)pl->steps, reinterpret_cast<A *>(pl->tw));
+                                                                       (long long)pl->steps, reinterpret_cast<A *>(pl->tw), lag);
     const long long total = (long long)pl->chunks * pl->n_recv * pl->nf;
     const size_t tiled_smem = (size_t)wk::RING * wk::dft_nfp((int)pl->nf) * sizeof(float2);
     bool tiled = false;
@@ -797,41 +805,44 @@ void launch_fold(wavey_cuda_plan *pl, int count) {
             const long long threads = (long long)pl->chunks * (wk::dft_nfp((int)pl->nf) / wk::DFT_FB) * pl->n_recv;
             wk::dft_chunk_tiled<V><<<(unsigned)((threads + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, tiled_smem, s>>>(
                 reinterpret_cast<const float *>(pl->ring), reinterpret_cast<const float *>(pl->tw), pl->acc,
-                (int)pl->n_recv, (int)pl->nf, pl->chunks, count, pl->base, (long long)pl->steps);
+                (int)pl->n_recv, (int)pl->nf, pl->chunks, count, pl->base, (long long)pl->steps, lag, pl->ring_stride);
             tiled = true;
         }
     }
     if (!tiled && total > 0)
         wk::dft_chunk<T, V, A><<<(unsigned)((total + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
             reinterpret_cast<const T *>(pl->ring), reinterpret_cast<const A *>(pl->tw), pl->acc, (int)pl->n_recv, (int)pl->nf,
-            pl->chunks, count, pl->base, (long long)pl->steps);
+            pl->chunks, count, pl->base, (long long)pl->steps, lag, pl->ring_stride);
     if (pl->want_ir) {
         const long long n = (long long)pl->chunks * V * pl->n_recv * count;
         if (n > 0)
             wk::ir_chunk<T, V><<<(unsigned)((n + wk::BLOCK - 1) / wk::BLOCK), wk::BLOCK, 0, s>>>(
                 reinterpret_cast<const T *>(pl->ring), reinterpret_cast<T *>(pl->ir), (int)pl->n_recv, pl->chunks,
-                pl->n_sources, (long long)pl->steps, pl->base, count);
+                pl->n_sources, (long long)pl->steps, pl->base, count, lag, pl->ring_stride);
     }
 }
 
-void fold(wavey_cuda_plan *pl, int count) {
+// The receiver fold of the chunk that starts at step *base - lag (lag 0: the
+// chunk just run; RING: the one before it), on stream s (default: the plan's).
+void fold(wavey_cuda_plan *pl, int count, int lag = 0, cudaStream_t s = nullptr) {
+    if (!s) s = pl->ctx->stream;
     if (pl->precision == WAVEY_FP64) {  // FP32 and FP16 storage fold in FP32
         switch (pl->V) {
-            case 1: launch_fold<double, 1>(pl, count); break;
-            case 2: launch_fold<double, 2>(pl, count); break;
-            default: launch_fold<double, 4>(pl, count); break;
+            case 1: launch_fold<double, 1>(pl, count, lag, s); break;
+            case 2: launch_fold<double, 2>(pl, count, lag, s); break;
+            default: launch_fold<double, 4>(pl, count, lag, s); break;
         }
     } else if (pl->dft64) {  // FP32 samples, FP64 twiddles and chunk sums
         switch (pl->V) {
-            case 1: launch_fold<float, 1, double>(pl, count); break;
-            case 2: launch_fold<float, 2, double>(pl, count); break;
-            default: launch_fold<float, 4, double>(pl, count); break;
+            case 1: launch_fold<float, 1, double>(pl, count, lag, s); break;
+            case 2: launch_fold<float, 2, double>(pl, count, lag, s); break;
+            default: launch_fold<float, 4, double>(pl, count, lag, s); break;
         }
     } else {
         switch (pl->V) {
-            case 1: launch_fold<float, 1>(pl, count); break;
-            case 2: launch_fold<float, 2>(pl, count); break;
-            default: launch_fold<float, 4>(pl, count); break;
+            case 1: launch_fold<float, 1>(pl, count, lag, s); break;
+            case 2: launch_fold<float, 2>(pl, count, lag, s); break;
+            default: launch_fold<float, 4>(pl, count, lag, s); break;
         }
     }
 }
@@ -843,12 +854,23 @@ int build_graph(wavey_cuda_plan *pl) {
     int st = ctx->cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
     if (st) return st;
     cudaEventRecordWithFlags(pl->ev_a, s, cudaEventRecordExternal);
+    if (pl->fold_overlap) {
+        // The previous chunk's fold beside this chunk's steps (nothing in
+        // the first chunk); the two use different rings.
+        cudaEventRecord(pl->ev_ffork, s);
+        cudaStreamWaitEvent(ctx->folds, pl->ev_ffork, 0);
+        fold(pl, wk::RING, wk::RING, ctx->folds);
+        cudaEventRecord(pl->ev_fjoin, ctx->folds);
+    }
     if (pl->tb2)
         for (int t = 0; t < wk::RING; t += 2) launch_pair_tb2(pl, t, (t >> 1) & 1);
     else
         for (int t = 0; t < wk::RING; t++) step(pl, t, t & 1);
     cudaEventRecordWithFlags(pl->ev_b, s, cudaEventRecordExternal);
-    fold(pl, wk::RING);
+    if (pl->fold_overlap)
+        cudaStreamWaitEvent(s, pl->ev_fjoin, 0);
+    else
+        fold(pl, wk::RING);
     wk::advance_base<<<1, 1, 0, s>>>(pl->base, wk::RING);
     cudaError_t e = cudaStreamEndCapture(s, &g);
     if (e != cudaSuccess) return ctx->cuda(e, "end capture");
@@ -1479,7 +1501,12 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     }
     if ((st = upload(pl, &pl->recv, recv_p.data(), recv_p.size() * 4))) return bail(st);
     if ((st = upload(pl, &pl->freqs, freqs, nf * sizeof(double)))) return bail(st);
-    if ((st = alloc(pl, &pl->ring, (size_t)pl->chunks * wk::RING * n_recv * pl->V * E))) return bail(st);
+    // Standalone plans that run 128-step graphs get two rings (each chunk folds
+    // the previous one beside its own steps).
+    pl->fold_overlap = standalone && steps >= (size_t)wk::RING && env_int("WAVEY_FOLD_OVERLAP", 1, 0, 1) != 0;
+    const int64_t ring_elems = (int64_t)pl->chunks * wk::RING * (int64_t)n_recv * pl->V;
+    pl->ring_stride = pl->fold_overlap ? ring_elems : 0;
+    if ((st = alloc(pl, &pl->ring, (size_t)ring_elems * (pl->fold_overlap ? 2 : 1) * E))) return bail(st);
     pl->dft64 = precision != WAVEY_FP64 && env_int("WAVEY_DFT_FP64", 0, 0, 1);
     if ((st = alloc(pl, &pl->tw, (size_t)wk::RING * nf * 2 * (pl->dft64 ? sizeof(double) : E)))) return bail(st);
     pl->acc_bytes = (size_t)pl->chunks * n_recv * nf * pl->V * 2 * sizeof(double);
@@ -1492,7 +1519,7 @@ int plan_create(wavey_cuda_ctx *ctx, const wavey_grid *grid, const wavey_source 
     for (cudaEvent_t *e : {&pl->ev_a, &pl->ev_b, &pl->ev_t0, &pl->ev_t1, &pl->inflight[0], &pl->inflight[1], &pl->inflight[2],
                            &pl->inflight[3]})
         if ((st = ctx->cuda(cudaEventCreate(e), "event create"))) return bail(st);
-    for (cudaEvent_t *e : {&pl->ev_fork, &pl->ev_join})
+    for (cudaEvent_t *e : {&pl->ev_fork, &pl->ev_join, &pl->ev_ffork, &pl->ev_fjoin})
         if ((st = ctx->cuda(cudaEventCreateWithFlags(e, cudaEventDisableTiming), "event create"))) return bail(st);
     if ((st = alloc(pl, &pl->err, sizeof(int)))) return bail(st);
     if (standalone && (precision == WAVEY_FP32 || precision == WAVEY_FP16_STORAGE) && tma_selected()) {
@@ -1602,6 +1629,8 @@ int plan_run(wavey_cuda_plan *pl, const volatile int32_t *cancel, void (*progres
         }
         if (progress) progress((double)((c + 1) * wk::RING) / (double)pl->steps, user);
     }
+    // The last full chunk's fold (the graphs fold each chunk in the next one).
+    if (pl->fold_overlap && full > 0) fold(pl, wk::RING, wk::RING);
     if (rem > 0) {
         if (cancel && *cancel) {
             cudaStreamSynchronize(s);
@@ -2394,7 +2423,8 @@ int wavey_cuda_create(int device, wavey_cuda_ctx **out) {
     if (!ctx) return WAVEY_E_NOMEM;
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->folds, cudaStreamNonBlocking) != cudaSuccess) {
         cudaGetLastError();
         delete ctx;
         return WAVEY_E_CUDA;
@@ -2428,6 +2458,7 @@ void wavey_cuda_destroy(wavey_cuda_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->folds) cudaStreamDestroy(ctx->folds);
     delete ctx;
 }
 
